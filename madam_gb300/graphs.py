@@ -1,0 +1,109 @@
+"""Graph inputs for the Max-Cut bound: rudy edge lists and seeded generators.
+
+The rudy format is the reference's input (process_input.c:182-225): a header
+line ``n m`` followed by ``m`` lines ``i j w`` with 1-based vertices.  The
+extended objective matrix built from it (process_input.c:255-299) is
+
+    SP->L = [Lap, Lap e; (Lap e)^T, e^T Lap e]
+
+where Lap = Diag(A e) - A restricted to the first n-1 vertices (the last vertex
+is fixed to the 0 side of the cut) and A is the weighted adjacency matrix.
+
+The generators produce rudy-style families with seeded streams: G(n, p) with
+unit, +-1 or uniform-integer weights, and 2D toroidal grids (spin glasses).
+They follow the families' semantics (density, weight law), not rudy's own
+random streams, which are not available.
+"""
+import numpy as np
+
+
+def read_rudy(path):
+    """Return (n, edges[m,2] 1-based int32, weights[m] float64)."""
+    with open(path) as f:
+        toks = f.read().split()
+    n, m = int(toks[0]), int(toks[1])
+    a = np.array(toks[2:2 + 3 * m], dtype=np.float64).reshape(m, 3)
+    e = a[:, :2].astype(np.int32)
+    if m and (e.min() < 1 or e.max() > n):
+        raise ValueError("vertex out of range")
+    return n, e, a[:, 2].copy()
+
+
+def write_rudy(path, n, edges, w):
+    with open(path, "w") as f:
+        f.write("%d %d\n" % (n, len(w)))
+        for (i, j), x in zip(edges, w):
+            f.write("%d %d %g\n" % (i, j, x))
+
+
+def extended_laplacian(n, edges, w):
+    """SP->L of process_input.c:255-299 as an (n, n) array (symmetric)."""
+    A = np.zeros((n, n))
+    e = np.asarray(edges, dtype=np.int64) - 1
+    A[e[:, 0], e[:, 1]] = w
+    A[e[:, 1], e[:, 0]] = w
+    deg = A.sum(axis=1)
+    m = n - 1
+    L = np.zeros((n, n))
+    Lap = np.diag(deg[:m]) - A[:m, :m]
+    L[:m, :m] = Lap
+    # vector part: row sums of Lap taken in the reference's accumulation order
+    rs = np.array([sum(Lap[ii, jj] for jj in range(m)) for ii in range(m)]) if m <= 64 else Lap.sum(axis=1)
+    L[:m, m] = rs
+    L[m, :m] = rs
+    L[m, m] = rs.sum()
+    return L
+
+
+def gnp(n, p, weights="one", seed=0):
+    """Seeded G(n, p); weights: 'one', 'pm1' (uniform {-1,+1}) or 'int10' (uniform integers in [-10, 10],
+    zero weights kept as edges)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    iu, ju = np.triu_indices(n, k=1)
+    keep = rng.random(iu.size) < p
+    i, j = iu[keep] + 1, ju[keep] + 1
+    if weights == "one":
+        w = np.ones(i.size)
+    elif weights == "pm1":
+        w = rng.choice(np.array([-1.0, 1.0]), size=i.size)
+    elif weights == "int10":
+        w = rng.integers(-10, 11, size=i.size).astype(np.float64)
+    else:
+        raise ValueError(weights)
+    return n, np.stack([i, j], axis=1).astype(np.int32), w
+
+
+def torus2d(rows, cols, seed=0):
+    """2D toroidal grid with uniform {-1,+1} couplings (n = rows*cols, degree 4)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    ed = []
+    for r in range(rows):
+        for c in range(cols):
+            v = r * cols + c
+            ed.append((v, r * cols + (c + 1) % cols))
+            ed.append((v, ((r + 1) % rows) * cols + c))
+    ed = np.array(ed, dtype=np.int64)
+    lo = np.minimum(ed[:, 0], ed[:, 1]) + 1
+    hi = np.maximum(ed[:, 0], ed[:, 1]) + 1
+    w = rng.choice(np.array([-1.0, 1.0]), size=len(ed))
+    return rows * cols, np.stack([lo, hi], axis=1).astype(np.int32), w
+
+
+def cut_value(n, edges, w, side):
+    """Weight of the cut given a 0/1 side vector over the first n-1 vertices (last vertex on side 0)."""
+    s = np.zeros(n, dtype=np.int64)
+    s[: n - 1] = side[: n - 1]
+    e = np.asarray(edges, dtype=np.int64) - 1
+    return float(np.sum(np.asarray(w)[s[e[:, 0]] != s[e[:, 1]]]))
+
+
+def random_fixings(n, count, max_fixed, seed=0):
+    """`count` node fixings over the first n-1 vertices: 0..max_fixed fixed variables each."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    out = []
+    for _ in range(count):
+        k = int(rng.integers(0, max_fixed + 1))
+        idx = rng.choice(n - 1, size=k, replace=False) if k else np.zeros(0, dtype=np.int64)
+        val = rng.integers(0, 2, size=k)
+        out.append({int(i): int(v) for i, v in zip(idx, val)})
+    return out
