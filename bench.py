@@ -1,0 +1,322 @@
+#!/usr/bin/env python
+"""Benchmark of the GPU node bound (MADAM's Evaluate/SDPbound) on GB300.
+
+One step = one batched call that bounds a whole batch of branch-and-bound
+nodes (IPM + cutting-plane ADMM rounds + separations + safe bound per node) of
+the configured workload; the problem matrix is resident on the device.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME]
+  python bench.py --impl reference ...   # the reference's CPU method on the host cores
+
+Prints one JSON line (rank 0).  `value` is node bounds per second over the
+device-timed region (CUDA events on the library's stream); `e2e` is the same
+through the C ABI call with host buffers, timed on the host.
+"""
+import argparse
+import json
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = "node bounds/sec"
+UNIT = "nodes/s"
+
+
+def _args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="gnp256_pm1_batch64")
+    ap.add_argument("--proj", default="fp64", choices=["fp64"])
+    ap.add_argument("--cpu-sample", type=int, default=0, help="nodes in the CPU sample (0: one per core)")
+    ap.add_argument("--cpu-only", action="store_true", help=argparse.SUPPRESS)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------
+# CPU side: the oracle (the reference's method restated in C) on host cores
+def _cpu_worker(args):
+    wl_name, idx_list, lb = args
+    from madam_gb300 import workload as W
+    from oracle import oracle as O
+
+    wl = W.make(wl_name)
+    prm = O.shipped_params(**wl["params"])
+    out = []
+    for i in idx_list:
+        oc = O.Ctx(prm, wl["SL"], wl["n"], rng=O.RNG_COUNTER, topk=O.TOPK_CANONICAL, canon_sign=1)
+        oc.set_lb(lb)
+        nd = O.make_node(wl["n"] - 1, wl["fixings"][i])
+        t0 = time.perf_counter()
+        b, st = oc.evaluate(nd, rank=1)
+        out.append((i, b, time.perf_counter() - t0))
+        oc.close()
+    return out
+
+
+def cpu_sample(wl_name, nodes, cores):
+    # single-threaded BLAS per process, as the reference runs it (setupenv.sh:6-8)
+    for v in ("OPENBLAS_NUM_THREADS", "GOTO_NUM_THREADS", "OMP_NUM_THREADS"):
+        os.environ[v] = "1"
+    from madam_gb300 import workload as W
+
+    wl = W.make(wl_name)
+    nodes = min(nodes, len(wl["fixings"]))
+    chunks = [[i] for i in range(nodes)]
+    ctx = mp.get_context("spawn")
+    t0 = time.perf_counter()
+    with ctx.Pool(cores) as pool:
+        res = pool.map(_cpu_worker, [(wl_name, c, wl["lb"]) for c in chunks])
+    wall = time.perf_counter() - t0
+    per = [r for rr in res for r in rr]
+    return dict(nodes=nodes, wall=wall, cores=cores, value=nodes / wall,
+                node_seconds=statistics.mean(p[2] for p in per))
+
+
+def host_cores():
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
+
+
+# ---------------------------------------------------------------------------
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, index=0):
+        self.f = tempfile.NamedTemporaryFile(prefix="clocks", suffix=".csv", delete=False)
+        self.p = None
+        self.index = index
+
+    def start(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if self.p:
+            self.p.terminate()
+            try:
+                self.p.wait(timeout=5)
+            except Exception:
+                self.p.kill()
+        self.f.close()
+        sm, smax, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        try:
+            for line in open(self.f.name):
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    smax = max(smax, float(parts[2]))
+                except ValueError:
+                    continue
+                for nm, v in zip(names, parts[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(nm)
+            os.unlink(self.f.name)
+        except Exception:
+            pass
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        return json.load(open(os.path.join(HERE, "MEASURED_PEAKS.json")))
+    except Exception:
+        return {}
+
+
+# ---------------------------------------------------------------------------
+def run_ours(a):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    import torch
+
+    from madam_gb300 import lib as M
+    from madam_gb300 import workload as W
+
+    torch.cuda.set_device(local)
+    wl = W.make(a.workload)
+    stream = torch.cuda.Stream()
+    nodes_fix = wl["fixings"]
+    batch = len(nodes_fix)
+    prm = M.params(**wl["params"])
+    ctx = M.Context(prm, wl["SL"], wl["n"], batch_max=batch, flags=M.PROJ_FP64 | M.FLAG_PROFILE,
+                    stream=stream.cuda_stream)
+
+    base_trials = (prm.Pent_Trials, prm.Hepta_Trials)
+
+    def step():
+        # every step starts from the same state: incumbent and the Pent/Hepta_Trials
+        # that give-ups grow (bounding.c:184-187) reset
+        ctx.set_trials(*base_trials)
+        ctx.set_lb(wl["lb"], wl["lb_sol"])
+        nodes = [M.node(f) for f in nodes_fix]
+        b, st = ctx.bound_batch(nodes, rank=1)
+        return b, st
+
+    for _ in range(a.warmup):
+        step()
+    torch.cuda.synchronize()
+    ctx.reset_kernel_stats()
+    if dist:
+        dist.barrier()
+    clocks = Clocks(local)
+    clocks.start()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ev0.record(stream)
+    stats = []
+    for _ in range(a.steps):
+        b, st = step()
+        stats.append(st)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    if dist:
+        dist.barrier()
+    clk = clocks.stop()
+    dev_s = ev0.elapsed_time(ev1) / 1e3
+    launches = ctx.launch_count()
+    ks = ctx.kernel_stats()
+    kw = ctx.kernel_work()
+    h2d, d2h = ctx.transfer_stats()
+    if dist:
+        t = torch.tensor([dev_s, wall], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dev_s, wall = float(t[0]), float(t[1])
+    total_nodes = batch * a.steps * world
+    if rank != 0:
+        dist.destroy_process_group()
+        return
+    # roofline of the dominant kernel class
+    fp64_peak = M.fp64_peak_gflops()
+    peaks = measured_peaks()
+    dom = max(ks.items(), key=lambda kv: kv[1][1])
+    counted = {k: v for k, v in ks.items() if kw.get(k, (0, 0))[1] and v[1] > 0}
+    roof = None
+    name, (nl, ms) = dom
+    work, unit = kw.get(name, (0.0, 0))
+    if not unit and counted:
+        name, (nl, ms) = max(counted.items(), key=lambda kv: kv[1][1])
+        work, unit = kw[name]
+    if unit == 1:
+        ach = work / (ms / 1e3) / 1e12
+        roof = {"kernel": name, "bound": "fp64", "achieved": ach, "peak": fp64_peak / 1e3, "unit": "TFLOP/s",
+                "frac": ach / (fp64_peak / 1e3), "traffic": None, "launches": nl, "ms_per_launch": ms / max(nl, 1),
+                "peak_source": "measured FP64 FMA microbenchmark (no FP64 entry in the measured peaks file)"}
+    elif unit == 2:
+        hbm = peaks.get("hbm_gbs", 6800.0)
+        ach = work / (ms / 1e3) / 1e9
+        roof = {"kernel": name, "bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
+                "traffic": None, "launches": nl, "ms_per_launch": ms / max(nl, 1),
+                "peak_source": "measured" if "hbm_gbs" in peaks else "fallback"}
+    share = {k: round(v[1] / max(1e-9, sum(x[1] for x in ks.values())), 4) for k, v in ks.items() if v[0]}
+    cpu = None
+    if not a.no_cpu_baseline:
+        cores = host_cores()
+        ns = a.cpu_sample or cores
+        r = subprocess.run([sys.executable, os.path.join(HERE, "bench.py"), "--cpu-only", "--workload", a.workload,
+                            "--cpu-sample", str(ns)], capture_output=True, text=True)
+        try:
+            c = json.loads(r.stdout.strip().splitlines()[-1])
+            cpu = {"value": c["value"], "unit": UNIT, "cores": c["cores"], "kind": "port",
+                   "sample": "%d of the workload's nodes, one per process, oracle (C restatement of the reference) "
+                             "with single-threaded OpenBLAS; %.1f s wall" % (c["nodes"], c["wall"])}
+        except Exception:
+            cpu = {"value": None, "unit": UNIT, "cores": None, "kind": "port", "sample": "failed: " + r.stderr[-300:]}
+    admm = sum(s.admm_iters for st in stats for s in st)
+    out = {
+        "metric": METRIC, "value": total_nodes / dev_s, "unit": UNIT, "n_gpus": world, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": dev_s * 1e3 / a.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded rudy-style G(n,p) graph and node fixings)",
+        "config": {"workload": a.workload, "n": wl["n"], "nodes_per_step": batch, "projection": "fp64 eigensolver",
+                   "cuts": "tri+pent" if not wl["params"].get("include_Hepta", 1) else "tri+pent+hept",
+                   "params": "reference shipped params file, " + ", ".join("%s=%s" % kv for kv in wl["params"].items()),
+                   "incumbent": wl["lb"], "l2": "working set per step > L2 (64 nodes x 8 n^2 FP64 buffers)",
+                   "parallelism": "replicas" if world > 1 else "single"},
+        "e2e": {"value": total_nodes / wall, "unit": UNIT, "h2d_bytes_per_step": h2d // a.steps,
+                "d2h_bytes_per_step": d2h // a.steps},
+        "gpu_launches": launches,
+        "roofline": roof,
+        "kernel_time_share": share,
+        "admm_iters_per_step": admm // a.steps,
+        "cpu_baseline": cpu,
+        "clocks": clk,
+    }
+    print(json.dumps(out))
+    if dist:
+        dist.destroy_process_group()
+
+
+def run_reference(a):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    cores = host_cores()
+    ns = a.cpu_sample or cores
+    vals = []
+    for i in range(a.warmup + a.steps):
+        r = cpu_sample(a.workload, ns if i >= a.warmup else 1, cores)
+        if i >= a.warmup:
+            vals.append(r)
+    tot_nodes = sum(r["nodes"] for r in vals)
+    tot_wall = sum(r["wall"] for r in vals)
+    v = tot_nodes / tot_wall
+    out = {
+        "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
+        "steps": a.steps, "warmup": a.warmup, "ms_per_step": tot_wall * 1e3 / a.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+        "config": {"workload": a.workload, "nodes_per_step": ns},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": "%d nodes per step, one process per core, oracle (C restatement of the "
+                                   "reference, checked bit-for-bit against it) with single-threaded OpenBLAS" % ns},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out))
+
+
+def main():
+    a = _args()
+    if a.cpu_only:
+        r = cpu_sample(a.workload, a.cpu_sample or host_cores(), host_cores())
+        print(json.dumps(r))
+        return
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_ours(a)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,186 @@
+/*
+ * mcbound.h -- C ABI of the GB300 (sm_103a) node-bound library for the MADAM
+ * exact Max-Cut branch-and-bound.
+ *
+ * The library replaces MADAM's bound call:
+ *     double Evaluate(BabNode *node, Problem *SP, Problem *PP, int rank)
+ * (admm.h:246, evaluate.c:12-21) and everything below it: createSubproblem
+ * (evaluate.c:39-116), SDPbound (bounding.c:25-250), the basic-SDP IPM
+ * (ipm_mc_pk.c), ADMM with the safe bound (admm.c:49-771), the cut operators and
+ * PSD projection (operators.c) and the triangle / pentagonal / heptagonal
+ * separation (cutting_planes.c, qap_simulated_annealing.c).  The GW + 1-opt
+ * heuristic that SDPbound calls (heuristic.c) runs on the host inside the
+ * library on the GPU's eigen factor.
+ *
+ * Conventions: plain pointers and sizes, host memory in and out; device memory
+ * is owned by the context; every entry point returns a status code (MCB_OK = 0
+ * or a negative MCB_ERR_*), never exits and never traps the GPU.  One context
+ * per host thread; a context is not re-entrant.  Matrices are column-major.
+ */
+#ifndef MCBOUND_H
+#define MCBOUND_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MCB_NMAX 1024     /* admm.h:131 NMAX */
+#define MCB_MAX_TRI 50000 /* admm.h:34 */
+#define MCB_MAX_PENT 50000
+#define MCB_MAX_HEPT 50000
+
+enum mcb_status {
+    MCB_OK = 0,
+    MCB_ERR_ARG = -1,      /* invalid argument or size beyond the stated limit   */
+    MCB_ERR_CUDA = -2,     /* CUDA runtime error (message in mcb_last_error)     */
+    MCB_ERR_NOMEM = -3,    /* device or host allocation failed                   */
+    MCB_ERR_NUMERIC = -4,  /* factorisation failed / non-finite values           */
+    MCB_ERR_CAPACITY = -5, /* a cut or candidate buffer would overflow           */
+    MCB_ERR_ITER = -6,     /* a device iteration cap was reached (CG, bisection) */
+    MCB_ERR_NODEV = -7     /* no CUDA device                                     */
+};
+
+/* Projection forms (mcb_create flags, low byte) */
+#define MCB_PROJ_FP64 0x0      /* plain: FP64 tridiagonal eigensolver (dsyevr's method) */
+#define MCB_PROJ_NS_BF16 0x1   /* chosen: BF16 Newton-Schulz sign iteration + FP64 refinement */
+#define MCB_PROJ_NS_TF32 0x2   /* chosen: TF32 Newton-Schulz sign iteration + FP64 refinement */
+/* Other flags */
+#define MCB_FLAG_PROFILE 0x100 /* time every kernel class with CUDA events */
+#define MCB_FLAG_LEARNED 0x200 /* learned cut ranking + dual warm start (needs mcb_load_model) */
+
+/* Same fields, order and meaning as MADAM's Parameters (admm.h:57-89). */
+typedef struct mcb_params {
+    double sigma0;
+    double scaleSigma;
+    int ADMM_itermax;
+    double tol0;
+    double scaleTol;
+    double minTol;
+    int triag_iter;
+    int pent_iter;
+    int hept_iter;
+    int max_outer_iter;
+    int extra_iter;
+    double violated_TriIneq;
+    int TriIneq;
+    int adjust_TriIneq;
+    int PentIneq;
+    int HeptaIneq;
+    int Pent_Trials;
+    int Hepta_Trials;
+    int include_Pent;
+    int include_Hepta;
+    int root;
+    int use_diff;
+    int branchingStrategy;
+} mcb_params;
+
+/* Same layout as MADAM's BabNode (admm.h:147-155), so a BabNode* can be passed. */
+typedef struct mcb_bab_node {
+    int xfixed[MCB_NMAX];
+    int sol[MCB_NMAX];
+    double fracsol[MCB_NMAX];
+    int level;
+    double upper_bound;
+} mcb_bab_node;
+
+/* Per-node counters returned by the bound calls. */
+typedef struct mcb_node_stats {
+    double bound;       /* f + fixedvalue (what Evaluate returns)          */
+    double basic_bound; /* IPM bound + fixedvalue                          */
+    int n_sub;          /* subproblem size                                 */
+    int outer_iters;    /* cutting-plane rounds                            */
+    int admm_iters;     /* ADMM iterations, all rounds                     */
+    int ipm_iters;      /* IPM iterations                                  */
+    int n_tri, n_pent, n_hept; /* cuts in the final relaxation             */
+    int pruned, gaveup;
+    double seconds;     /* wall time of the batch call this node was in    */
+} mcb_node_stats;
+
+typedef struct mcb_ctx mcb_ctx;
+
+/* ---- context ----------------------------------------------------------------
+ * SL is MADAM's SP->L (N x N extended Laplacian, process_input.c:255-299), N <= 1024.
+ * batch_max: most nodes bounded together by mcb_bound_batch.
+ * stream: a cudaStream_t to launch on (NULL: the context creates its own). */
+mcb_ctx *mcb_create(const mcb_params *params, int N, const double *SL, int batch_max, int flags,
+                    void *stream, int *status);
+void mcb_destroy(mcb_ctx *ctx);
+const char *mcb_strerror(int status);
+const char *mcb_last_error(const mcb_ctx *ctx);
+int mcb_version(void);
+
+/* Global state SDPbound reads and writes in MADAM: incumbent (Bab_LBGet/Bab_LBUpd,
+ * heap.c:15,185), diff (bounding.c:241-243), Pent/Hepta_Trials (bounding.c:184-187). */
+void mcb_set_lb(mcb_ctx *ctx, double lb, const int *sol);
+double mcb_get_lb(const mcb_ctx *ctx, int *sol);
+void mcb_set_diff(mcb_ctx *ctx, double diff);
+double mcb_get_diff(const mcb_ctx *ctx);
+void mcb_set_trials(mcb_ctx *ctx, int pent_trials, int hepta_trials);
+void mcb_get_trials(const mcb_ctx *ctx, int *pent_trials, int *hepta_trials);
+
+/* ---- the bound ---------------------------------------------------------------
+ * mcb_evaluate: Evaluate(node, SP, PP, rank) (evaluate.c:12).  Writes
+ * node->fracsol, updates the incumbent, returns the bound in *bound.
+ * mcb_bound_batch: the same for `count` independent nodes in one batched pass;
+ * the incumbent is shared (read at the start, updated as nodes find solutions). */
+int mcb_evaluate(mcb_ctx *ctx, mcb_bab_node *node, int rank, double *bound, mcb_node_stats *stats);
+int mcb_bound_batch(mcb_ctx *ctx, mcb_bab_node *const *nodes, int count, int rank, double *bounds,
+                    mcb_node_stats *stats);
+
+/* Serial-equivalent branch-and-bound driver (the MPI master/worker loop of
+ * main.c / bab_functions.c:226-334 as one process): root with rank 0 branched
+ * at once, then nodes popped in bound order `batch` at a time.  Returns status;
+ * *nodes counts as the reference does (1 + 2 per branching). */
+int mcb_bab(mcb_ctx *ctx, int batch, int max_nodes, double *opt, int *sol, double *root_bound,
+            int *nodes, mcb_node_stats *log, int log_cap, int *log_count);
+
+/* ---- operator-level entry points (host pointers; device memory per call) -----
+ * Cut arrays: tri = 4 ints per cut (i, j, k, type) with i > j > k (Triangle_Inequality,
+ * admm.h:93-100); pent = 6 ints (type, perm[5]); hept = 8 ints (type, perm[7]). */
+/* y += B(X), operators.c:62-150 (X read through its lower triangle) */
+int mcb_op_B(int n, const double *X, int ntri, const int *tri, int npent, const int *pent, int nhept,
+             const int *hept, double *y);
+/* X -= B^T(t), operators.c:171-513 */
+int mcb_op_Bt(int n, double *X, int ntri, const int *tri, int npent, const int *pent, int nhept,
+              const int *hept, const double *t);
+/* PSD projection, operators.c:521-619: W (lower) -> Xp = W_+ (full symmetric),
+ * Q = Xp - W (lower), Z = eigenvectors * sqrt(lambda) of the M eigenvalues > 1e-8
+ * (ascending), evals.  proj = MCB_PROJ_* form. */
+int mcb_project_psd(int n, const double *W, int proj, double *Xp, double *Q, double *Z, double *evals,
+                    int *M);
+/* largest eigenvalue (admm.c:731-752) and a rigorous upper bound on it */
+int mcb_lambda_max(int n, const double *A, double *lmax, double *lmax_upper);
+/* basic SDP relaxation by the predictor-corrector IPM, ipm_mc_pk.c */
+int mcb_ipm(int n, const double *L, double *X, double *y, double *Z, double *phi, int *iters);
+/* triangle separation, cutting_planes.c:48-127: the K most violated (> thr) in scan order */
+int mcb_separate_triangles(int n, const double *X, int K, double thr, int *out, double *vals, int *count,
+                           double *max_violation);
+/* k-gonal SA (qap_simulated_annealing.c) on X (full symmetric): trials * ntypes
+ * independent runs (ntypes = 3 for k = 5, 4 for k = 7), run r with type r % ntypes + 1
+ * and counter stream key2(key, (r / ntypes) * 8 + type) -- the runs of one
+ * getViolated_Pentagonal/HeptagonalInequalities call (cutting_planes.c:247-250,
+ * 444-447).  ineq: k ints per run; values: the SA cost per run. */
+int mcb_qap_sa_batch(int n, const double *X, int k, int trials, uint64_t key, int *ineq, double *values);
+
+/* ---- instrumentation ---------------------------------------------------------
+ * Per kernel class: launches and total device time (ms, CUDA events on the
+ * context's stream; needs MCB_FLAG_PROFILE).  Returns the number of classes. */
+int mcb_kernel_stats(const mcb_ctx *ctx, int cap, char (*names)[32], long long *launches, double *ms);
+void mcb_reset_kernel_stats(mcb_ctx *ctx);
+/* algorithmic work per kernel class, same order as mcb_kernel_stats: unit[i] = 1 for
+ * FP64 flops, 2 for bytes, 0 when the class has no counted work.  Counted from the
+ * iterations each node actually executed. */
+int mcb_kernel_work(const mcb_ctx *ctx, int cap, double *work, int *unit);
+/* host<->device bytes moved by the bound calls since the last reset */
+void mcb_transfer_stats(const mcb_ctx *ctx, long long *h2d_bytes, long long *d2h_bytes);
+/* FP64 FMA throughput of the current device in GFLOP/s (microbenchmark) */
+double mcb_measure_fp64_peak(void);
+long long mcb_launch_count(const mcb_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,509 @@
+// k_eig.cu -- FP64 symmetric eigensolver for the PSD projection (plain form).
+//
+// The reference projects with LAPACK dsyevr, RANGE='V' over (1e-8, VU]
+// (operators.c:521-619).  For a value range dsyevr reduces to tridiagonal form
+// (dsytrd), finds the eigenvalues by Sturm bisection (dstebz) and the vectors
+// by inverse iteration with re-orthogonalisation inside clusters (dstein), then
+// back-transforms (dormtr).  These kernels do the same four steps on the GPU,
+// one CTA per node, FP64 throughout, with full-precision bisection.
+#include "mcb_dev.cuh"
+#include "kernels.h"
+
+namespace mcb {
+
+// ---------------------------------------------------------------------------
+// W (lower triangle authoritative) -> A (full symmetric copy)
+__global__ void k_sym_copy(Slot *slots, int src, int gate) {
+    Slot &s = slots[blockIdx.y];
+    if (!gated(s, gate)) return;
+    int n = s.n;
+    const double *W = src == 0 ? s.W : s.A;
+    double *A = s.A;
+    int total = n * n;
+    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += gridDim.x * blockDim.x) {
+        int j = idx / n, i = idx - j * n;
+        A[idx] = i >= j ? W[i + (size_t)j * n] : W[j + (size_t)i * n];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Householder tridiagonalisation of A (full symmetric, overwritten).  On exit
+// d[0..n-1], e[0..n-2], tau[0..n-3]; reflector k has v[k+1] = 1 and
+// v[i] = A[i + k n] for i >= k+2.
+__global__ void __launch_bounds__(512) k_tridiag(Slot *slots, int gate) {
+    Slot &s = slots[blockIdx.x];
+    if (!gated(s, gate)) return;
+    const int n = s.n, tid = threadIdx.x, bs = blockDim.x;
+    double *A = s.A;
+    extern __shared__ double sh[];
+    double *v = sh, *w = sh + n, *red = sh + 2 * n;
+    for (int k = 0; k < n - 2; ++k) {
+        const int m = n - k - 1;
+        double *x = A + (k + 1) + (size_t)k * n;
+        double loc = 0.0;
+        for (int i = 1 + tid; i < m; i += bs) loc += x[i] * x[i];
+        double sig2 = block_sum(loc, red);
+        double alpha = x[0];
+        double beta, tau, scal;
+        if (sig2 == 0.0) {
+            beta = alpha;
+            tau = 0.0;
+            scal = 0.0;
+        } else {
+            beta = -copysign(sqrt(alpha * alpha + sig2), alpha);
+            tau = (beta - alpha) / beta;
+            scal = 1.0 / (alpha - beta);
+        }
+        for (int i = tid; i < m; i += bs) v[i] = i == 0 ? 1.0 : x[i] * scal;
+        __syncthreads();
+        if (tau != 0.0) {
+            const double *A22 = A + (k + 1) + (size_t)(k + 1) * n;
+            for (int i = tid; i < m; i += bs) {
+                double acc = 0.0;
+                for (int j = 0; j < m; ++j) acc += A22[i + (size_t)j * n] * v[j];
+                w[i] = tau * acc;
+            }
+            loc = 0.0;
+            for (int i = tid; i < m; i += bs) loc += w[i] * v[i];
+            double pv = block_sum(loc, red);
+            double K = -0.5 * tau * pv;
+            for (int i = tid; i < m; i += bs) w[i] += K * v[i];
+            __syncthreads();
+            double *U = A + (k + 1) + (size_t)(k + 1) * n;
+            for (int idx = tid; idx < m * m; idx += bs) {
+                int j = idx / m, i = idx - j * m;
+                U[i + (size_t)j * n] -= v[i] * w[j] + w[i] * v[j];
+            }
+        }
+        if (tid == 0) {
+            s.d[k] = A[k + (size_t)k * n];
+            s.e[k] = beta;
+            s.tau[k] = tau;
+        }
+        for (int i = 1 + tid; i < m; i += bs) x[i] = v[i];
+        __syncthreads();
+    }
+    if (tid == 0) {
+        if (n >= 2) {
+            s.d[n - 2] = A[(n - 2) + (size_t)(n - 2) * n];
+            s.d[n - 1] = A[(n - 1) + (size_t)(n - 1) * n];
+            s.e[n - 2] = A[(n - 1) + (size_t)(n - 2) * n];
+            s.tau[n - 2] = 0.0;
+        } else if (n == 1) {
+            s.d[0] = A[0];
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Sturm count: eigenvalues of T strictly below x
+__device__ __forceinline__ int sturm(const double *d, const double *e2, int n, double x, double pivmin) {
+    int cnt = 0;
+    double q = d[0] - x;
+    if (fabs(q) < pivmin) q = -pivmin;
+    if (q < 0) ++cnt;
+    for (int i = 1; i < n; ++i) {
+        q = d[i] - x - e2[i - 1] / q;
+        if (fabs(q) < pivmin) q = -pivmin;
+        if (q < 0) ++cnt;
+    }
+    return cnt;
+}
+
+// Eigenvalues of T above vl (ascending) into ev[0..M-1]; M into s.M.
+// largest_only: just the largest eigenvalue into s.lmax.
+__global__ void k_bisect(Slot *slots, double vl, int largest_only, int gate) {
+    Slot &s = slots[blockIdx.x];
+    if (!gated(s, gate)) return;
+    const int n = s.n, tid = threadIdx.x;
+    extern __shared__ double sh[];
+    double *d = sh, *e2 = sh + n, *red = sh + 2 * n;
+    __shared__ int c0;
+    double lo_g = 1e308, hi_g = -1e308, em = 0.0;
+    for (int i = tid; i < n; i += blockDim.x) {
+        d[i] = s.d[i];
+        double el = i > 0 ? fabs(s.e[i - 1]) : 0.0, er = i < n - 1 ? fabs(s.e[i]) : 0.0;
+        if (i < n - 1) {
+            e2[i] = s.e[i] * s.e[i];
+            em = fmax(em, e2[i]);
+        }
+        lo_g = fmin(lo_g, d[i] - el - er);
+        hi_g = fmax(hi_g, d[i] + el + er);
+    }
+    double gl = -block_max(-lo_g, red);
+    double gu = block_max(hi_g, red);
+    double emax = block_max(em, red);
+    const double pivmin = 2.2250738585072014e-308 * fmax(1.0, emax);
+    double tnorm = fmax(fabs(gl), fabs(gu));
+    gl -= 2.0 * tnorm * 2.220446049250313e-16 * n + 2.0 * pivmin;
+    gu += 2.0 * tnorm * 2.220446049250313e-16 * n + 2.0 * pivmin;
+    // dstebz with ABSTOL <= 0 stops at ULP * max(|gl|, |gu|) (plus the pivmin guard)
+    const double atol = 2.220446049250313e-16 * tnorm + 4.0 * pivmin;
+    if (largest_only) {
+        if (tid == 0) {
+            double lo = gl, hi = gu;
+            int it = 0;
+            for (; it < 200; ++it) {
+                double mid = 0.5 * (lo + hi);
+                if (mid <= lo || mid >= hi) break;
+                if (sturm(d, e2, n, mid, pivmin) >= n) hi = mid;  // all eigenvalues below mid
+                else lo = mid;
+                if (hi - lo <= 2.0 * 2.220446049250313e-16 * fmax(fabs(lo), fabs(hi)) + atol) break;
+            }
+            s.lmax = 0.5 * (lo + hi);
+            s.acc[ACC_LMAX_HI] = hi;  // upper end of the final bracket
+            if (it >= 200) s.status = -6;
+        }
+        return;
+    }
+    if (tid == 0) c0 = vl <= gl ? 0 : sturm(d, e2, n, vl, pivmin);
+    __syncthreads();
+    int M = n - c0;
+    if (tid == 0) s.M = M;
+    for (int j = tid; j < M; j += blockDim.x) {
+        int idx = c0 + j;
+        double lo = fmax(vl, gl), hi = gu;
+        int it = 0;
+        for (; it < 200; ++it) {
+            double mid = 0.5 * (lo + hi);
+            if (mid <= lo || mid >= hi) break;
+            if (sturm(d, e2, n, mid, pivmin) > idx) hi = mid;
+            else lo = mid;
+            if (hi - lo <= 2.0 * 2.220446049250313e-16 * fmax(fabs(lo), fabs(hi)) + atol) break;
+        }
+        if (it >= 200) s.status = -6;
+        s.ev[j] = 0.5 * (lo + hi);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Inverse iteration for the M eigenvectors of T (dstein's method): LU of
+// (T - lambda I) with partial pivoting, three solves from a fixed pseudo-random
+// start, modified Gram-Schmidt against earlier vectors of the same cluster
+// (eigenvalues closer than 1e-3 ||T||_1).  Vectors go to V (n x M).
+// Scratch per warp: 5 n doubles in s.dwork.
+__device__ void tri_lu(const double *d, const double *e, int n, double lam, double tiny, double *dl,
+                       double *dd, double *du, double *du2, double *piv) {
+    for (int i = 0; i < n; ++i) dd[i] = d[i] - lam;
+    for (int i = 0; i < n - 1; ++i) {
+        dl[i] = e[i];
+        du[i] = e[i];
+    }
+    for (int i = 0; i < n - 1; ++i) {
+        if (fabs(dd[i]) >= fabs(dl[i])) {
+            if (dd[i] == 0.0) dd[i] = tiny;
+            double fact = dl[i] / dd[i];
+            dl[i] = fact;
+            dd[i + 1] -= fact * du[i];
+            if (i < n - 2) du2[i] = 0.0;
+            piv[i] = 0.0;
+        } else {
+            double fact = dd[i] / dl[i];
+            dd[i] = dl[i];
+            dl[i] = fact;
+            double temp = du[i];
+            du[i] = dd[i + 1];
+            dd[i + 1] = temp - fact * dd[i + 1];
+            if (i < n - 2) {
+                du2[i] = du[i + 1];
+                du[i + 1] = -fact * du[i + 1];
+            }
+            piv[i] = 1.0;
+        }
+    }
+    for (int i = 0; i < n; ++i)
+        if (fabs(dd[i]) < tiny) dd[i] = dd[i] < 0 ? -tiny : tiny;
+}
+
+__device__ void tri_solve(int n, const double *dl, const double *dd, const double *du, const double *du2,
+                          const double *piv, double *b) {
+    for (int i = 0; i < n - 1; ++i) {
+        if (piv[i] == 0.0) {
+            b[i + 1] -= dl[i] * b[i];
+        } else {
+            double temp = b[i];
+            b[i] = b[i + 1];
+            b[i + 1] = temp - dl[i] * b[i];
+        }
+    }
+    b[n - 1] /= dd[n - 1];
+    if (n > 1) b[n - 2] = (b[n - 2] - du[n - 2] * b[n - 1]) / dd[n - 2];
+    for (int i = n - 3; i >= 0; --i) b[i] = (b[i] - du[i] * b[i + 1] - du2[i] * b[i + 2]) / dd[i];
+}
+
+__global__ void __launch_bounds__(256) k_invit(Slot *slots, int gate) {
+    Slot &s = slots[blockIdx.x];
+    if (!gated(s, gate)) return;
+    const int n = s.n, M = s.M, lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if (M <= 0) return;
+    extern __shared__ double sh[];
+    double *d = sh, *e = sh + n, *red = sh + 2 * n;
+    int *cstart = (int *)(red + 40);  // M+1 ints
+    __shared__ int ncl;
+    double nrm = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        d[i] = s.d[i];
+        if (i < n - 1) e[i] = s.e[i];
+        double el = i > 0 ? fabs(s.e[i - 1]) : 0.0, er = i < n - 1 ? fabs(s.e[i]) : 0.0;
+        nrm = fmax(nrm, fabs(s.d[i]) + el + er);
+    }
+    double onenrm = block_max(nrm, red);
+    double ortol = 1e-3 * onenrm;
+    double tiny = 2.220446049250313e-16 * fmax(onenrm, 1e-300);
+    if (threadIdx.x == 0) {
+        int c = 0;
+        for (int j = 0; j < M; ++j)
+            if (j == 0 || s.ev[j] - s.ev[j - 1] > ortol) cstart[c++] = j;
+        cstart[c] = M;
+        ncl = c;
+    }
+    __syncthreads();
+    double *scr = s.dwork + (size_t)wid * 6 * n;
+    double *dl = scr, *dd = scr + n, *du = scr + 2 * n, *du2 = scr + 3 * n, *piv = scr + 4 * n, *b = scr + 5 * n;
+    for (int cl = wid; cl < ncl; cl += nw) {
+        int j0 = cstart[cl], j1 = cstart[cl + 1];
+        for (int j = j0; j < j1; ++j) {
+            double lam = s.ev[j];
+            if (lane == 0) tri_lu(d, e, n, lam, tiny, dl, dd, du, du2, piv);
+            for (int i = lane; i < n; i += 32) {
+                uint64_t h = mix64(((uint64_t)(j + 1) << 32) ^ (uint64_t)(i + 1));
+                b[i] = 2.0 * ((double)(h >> 11) * 0x1.0p-53) - 1.0;
+            }
+            __syncwarp();
+            double *vj = s.V + (size_t)j * n;
+            for (int it = 0; it < 3; ++it) {
+                if (lane == 0) tri_solve(n, dl, dd, du, du2, piv, b);
+                __syncwarp();
+                double ss = 0.0;
+                for (int i = lane; i < n; i += 32) ss += b[i] * b[i];
+                ss = warp_sum(ss);
+                double inv = ss > 0 ? 1.0 / sqrt(ss) : 0.0;
+                for (int i = lane; i < n; i += 32) b[i] *= inv;
+                __syncwarp();
+                for (int jp = j0; jp < j; ++jp) {
+                    const double *vp = s.V + (size_t)jp * n;
+                    double dot = 0.0;
+                    for (int i = lane; i < n; i += 32) dot += vp[i] * b[i];
+                    dot = warp_sum(dot);
+                    for (int i = lane; i < n; i += 32) b[i] -= dot * vp[i];
+                    __syncwarp();
+                }
+                if (j > j0) {
+                    ss = 0.0;
+                    for (int i = lane; i < n; i += 32) ss += b[i] * b[i];
+                    ss = warp_sum(ss);
+                    inv = ss > 0 ? 1.0 / sqrt(ss) : 0.0;
+                    for (int i = lane; i < n; i += 32) b[i] *= inv;
+                    __syncwarp();
+                }
+            }
+            for (int i = lane; i < n; i += 32) vj[i] = b[i];
+            __syncwarp();
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// V (n x M) <- Q V with Q = H_0 H_1 ... H_{n-3} (dormtr).
+__global__ void __launch_bounds__(256) k_backtrans(Slot *slots, int gate) {
+    Slot &s = slots[blockIdx.x];
+    if (!gated(s, gate)) return;
+    const int n = s.n, M = s.M, lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if (M <= 0 || n < 3) return;
+    extern __shared__ double sh[];
+    double *v = sh, *sc = sh + n;
+    const double *A = s.A;
+    double *V = s.V;
+    for (int k = n - 3; k >= 0; --k) {
+        double tau = s.tau[k];
+        if (tau == 0.0) continue;
+        const int m = n - k - 1;
+        for (int i = threadIdx.x; i < m; i += blockDim.x) v[i] = i == 0 ? 1.0 : A[(k + 1 + i) + (size_t)k * n];
+        __syncthreads();
+        for (int c = wid; c < M; c += nw) {
+            const double *col = V + (size_t)c * n + k + 1;
+            double acc = 0.0;
+            for (int i = lane; i < m; i += 32) acc += v[i] * col[i];
+            acc = warp_sum(acc);
+            if (lane == 0) sc[c] = tau * acc;
+        }
+        __syncthreads();
+        for (int idx = threadIdx.x; idx < m * M; idx += blockDim.x) {
+            int c = idx / m, i = idx - c * m;
+            V[(size_t)c * n + k + 1 + i] -= sc[c] * v[i];
+        }
+        __syncthreads();
+    }
+}
+
+// Canonical sign (largest-magnitude entry positive, first on ties) and scaling
+// of column j by sqrt(ev[j]) * extra (extra = 1, or sqrt(sigma) for the factor
+// the heuristic reads, admm.c:582-585).
+__global__ void k_canon_scale(Slot *slots, int gate) {
+    Slot &s = slots[blockIdx.y];
+    if (!gated(s, gate)) return;
+    const int n = s.n, M = s.M, lane = threadIdx.x & 31;
+    const int c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (c >= M) return;
+    double *col = s.V + (size_t)c * n;
+    double best = -1.0;
+    int arg = n;
+    for (int i = lane; i < n; i += 32) {
+        double a = fabs(col[i]);
+        if (a > best) { best = a; arg = i; }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        double ob = __shfl_xor_sync(0xffffffffu, best, o);
+        int oa = __shfl_xor_sync(0xffffffffu, arg, o);
+        if (ob > best || (ob == best && oa < arg)) { best = ob; arg = oa; }
+    }
+    double sgn = col[arg] < 0 ? -1.0 : 1.0;
+    double sc = sgn * sqrt(s.ev[c]);
+    for (int i = lane; i < n; i += 32) col[i] *= sc;
+}
+
+// ---------------------------------------------------------------------------
+// X+ = Y Y^T (Y = V after k_canon_scale, n x M) on 32x32 lower tiles, with the
+// epilogue of the caller:
+//   mode 0 (projection only): Xp = X+ full symmetric into s.X, Q = X+ - W lower into s.Q
+//   mode 1 (ADMM step, admm.c:574-585 and the residual terms of :600-665):
+//           X <- sigma X+ (full), Q <- X+ - W (full), partial sums per tile
+//           of ||X+ - X_old/sigma||^2, <L, X>, ||diag X - 1||^2 into s.dwork2
+constexpr int TS = 32;
+__global__ void __launch_bounds__(256) k_syrk_post(Slot *slots, int mode, double *partials, int ptile) {
+    Slot &s = slots[blockIdx.y];
+    if (!gated(s, mode)) return;
+    const int n = s.n, M = s.M;
+    const int nt = (n + TS - 1) / TS;
+    const int tile = blockIdx.x;
+    if (tile >= nt * (nt + 1) / 2) return;
+    int ti = 0;
+    while ((ti + 1) * (ti + 2) / 2 <= tile) ++ti;
+    int tj = tile - ti * (ti + 1) / 2;
+    const int i0 = ti * TS, j0 = tj * TS;
+    __shared__ double Ya[16][TS + 1], Yb[16][TS + 1];
+    __shared__ double red[40];
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8 threads, 4 rows each
+    double acc[4] = {0, 0, 0, 0};
+    const double *Y = s.V;
+    for (int k0 = 0; k0 < M; k0 += 16) {
+        for (int q = threadIdx.x; q < 16 * TS; q += blockDim.x) {
+            int kk = q / TS, r = q - kk * TS;
+            int ia = i0 + r, ja = j0 + r, kc = k0 + kk;
+            Ya[kk][r] = (ia < n && kc < M) ? Y[ia + (size_t)kc * n] : 0.0;
+            Yb[kk][r] = (ja < n && kc < M) ? Y[ja + (size_t)kc * n] : 0.0;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < 16; ++kk) {
+            double bj = Yb[kk][tx];
+#pragma unroll
+            for (int r = 0; r < 4; ++r) acc[r] += Ya[kk][ty * 4 + r] * bj;
+        }
+        __syncthreads();
+    }
+    double p_dres = 0.0, p_primal = 0.0, p_diag = 0.0;
+    const double sg = s.sigma;
+    for (int r = 0; r < 4; ++r) {
+        int i = i0 + ty * 4 + r, j = j0 + tx;
+        if (i >= n || j >= n || i < j) continue;
+        double xp = acc[r];
+        size_t ij = i + (size_t)j * n, ji = j + (size_t)i * n;
+        double w = s.W[ij];
+        if (mode == 0) {
+            s.X[ij] = xp;
+            s.X[ji] = xp;
+            s.Q[ij] = xp - w;
+        } else {
+            double xo = s.X[ij];
+            double xn = sg * xp;
+            double q = xp - w;
+            s.X[ij] = xn;
+            s.X[ji] = xn;
+            s.Q[ij] = q;
+            s.Q[ji] = q;
+            double dr = xp - xo / sg;
+            double mult = i == j ? 1.0 : 2.0;
+            p_dres += mult * dr * dr;
+            p_primal += mult * s.L[ij] * xn;
+            if (i == j) p_diag += (xn - 1.0) * (xn - 1.0);
+        }
+    }
+    if (mode == 1) {
+        double a = block_sum(p_dres, red);
+        double b = block_sum(p_primal, red);
+        double c = block_sum(p_diag, red);
+        if (threadIdx.x == 0) {
+            double *pp = partials + ((size_t)blockIdx.y * ptile + tile) * 3;
+            pp[0] = a;
+            pp[1] = b;
+            pp[2] = c;
+        }
+    }
+}
+
+// Sum the per-tile partials of k_syrk_post in a fixed order.
+__global__ void k_syrk_reduce(Slot *slots, const double *partials, int ptile) {
+    Slot &s = slots[blockIdx.x];
+    if (!gated(s, 1)) return;
+    const int nt = (s.n + TS - 1) / TS, T = nt * (nt + 1) / 2;
+    __shared__ double red[40];
+    double a = 0, b = 0, c = 0;
+    for (int t = threadIdx.x; t < T; t += blockDim.x) {
+        const double *pp = partials + ((size_t)blockIdx.x * ptile + t) * 3;
+        a += pp[0];
+        b += pp[1];
+        c += pp[2];
+    }
+    a = block_sum(a, red);
+    b = block_sum(b, red);
+    c = block_sum(c, red);
+    if (threadIdx.x == 0) {
+        s.acc[ACC_DRES2] = a;
+        s.acc[ACC_PRIMAL] = b;
+        s.acc[ACC_DIAG2] = c;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host-side launchers
+void launch_sym_copy(Slot *d_slots, int nslots, int nmax, int src, int gate, cudaStream_t st) {
+    dim3 g((nmax * nmax + 255) / 256 < 1024 ? (nmax * nmax + 255) / 256 : 1024, nslots);
+    k_sym_copy<<<g, 256, 0, st>>>(d_slots, src, gate);
+}
+void launch_tridiag(Slot *d_slots, int nslots, int nmax, int gate, cudaStream_t st) {
+    size_t sm = (2 * (size_t)nmax + 40) * sizeof(double);
+    k_tridiag<<<nslots, 512, sm, st>>>(d_slots, gate);
+}
+void launch_bisect(Slot *d_slots, int nslots, int nmax, double vl, int largest_only, int gate,
+                   cudaStream_t st) {
+    size_t sm = (2 * (size_t)nmax + 40) * sizeof(double);
+    k_bisect<<<nslots, 256, sm, st>>>(d_slots, vl, largest_only, gate);
+}
+void launch_invit(Slot *d_slots, int nslots, int nmax, int gate, cudaStream_t st) {
+    size_t sm = (2 * (size_t)nmax + 40) * sizeof(double) + ((size_t)nmax + 1) * sizeof(int);
+    k_invit<<<nslots, 256, sm, st>>>(d_slots, gate);
+}
+void launch_backtrans(Slot *d_slots, int nslots, int nmax, int gate, cudaStream_t st) {
+    size_t sm = (2 * (size_t)nmax) * sizeof(double);
+    k_backtrans<<<nslots, 256, sm, st>>>(d_slots, gate);
+}
+void launch_canon_scale(Slot *d_slots, int nslots, int nmax, int gate, cudaStream_t st) {
+    dim3 g((nmax + 7) / 8, nslots);
+    k_canon_scale<<<g, 256, 0, st>>>(d_slots, gate);
+}
+int syrk_tiles(int nmax) {
+    int nt = (nmax + TS - 1) / TS;
+    return nt * (nt + 1) / 2;
+}
+void launch_syrk_post(Slot *d_slots, int nslots, int nmax, int mode, double *partials, cudaStream_t st) {
+    int T = syrk_tiles(nmax);
+    dim3 g(T, nslots);
+    k_syrk_post<<<g, 256, 0, st>>>(d_slots, mode, partials, T);
+    if (mode == 1) k_syrk_reduce<<<nslots, 256, 0, st>>>(d_slots, partials, T);
+}
+
+size_t eig_dwork_doubles(int nmax) { return (size_t)8 * 6 * nmax; }
+
+}  // namespace mcb

@@ -1,0 +1,313 @@
+"""ctypes binding of libmcbound.so (the C ABI in include/mcbound.h).
+
+This is the Python mirror of the reference's bound interface: ``Context.evaluate``
+is MADAM's ``Evaluate(node, SP, PP, rank)`` (evaluate.c:12), ``Context.bound_batch``
+bounds many nodes in one batched pass, ``Context.bab`` is the branch-and-bound
+driver.  The library must be built (``madam_gb300.build.build()``); there is no
+fallback: a missing library or a missing CUDA device raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libmcbound.so")
+NMAX = 1024
+
+OK, ERR_ARG, ERR_CUDA, ERR_NOMEM, ERR_NUMERIC, ERR_CAPACITY, ERR_ITER, ERR_NODEV = 0, -1, -2, -3, -4, -5, -6, -7
+PROJ_FP64, PROJ_NS_BF16, PROJ_NS_TF32 = 0x0, 0x1, 0x2
+FLAG_PROFILE, FLAG_LEARNED = 0x100, 0x200
+
+PARAM_FIELDS = [
+    ("sigma0", C.c_double), ("scaleSigma", C.c_double), ("ADMM_itermax", C.c_int),
+    ("tol0", C.c_double), ("scaleTol", C.c_double), ("minTol", C.c_double),
+    ("triag_iter", C.c_int), ("pent_iter", C.c_int), ("hept_iter", C.c_int),
+    ("max_outer_iter", C.c_int), ("extra_iter", C.c_int), ("violated_TriIneq", C.c_double),
+    ("TriIneq", C.c_int), ("adjust_TriIneq", C.c_int), ("PentIneq", C.c_int),
+    ("HeptaIneq", C.c_int), ("Pent_Trials", C.c_int), ("Hepta_Trials", C.c_int),
+    ("include_Pent", C.c_int), ("include_Hepta", C.c_int), ("root", C.c_int),
+    ("use_diff", C.c_int), ("branchingStrategy", C.c_int),
+]
+
+# defaults of the reference's shipped parameter file (params:1-23)
+SHIPPED = dict(sigma0=1.0, scaleSigma=1.001, ADMM_itermax=2000, tol0=5e-2, scaleTol=0.6, minTol=1e-3,
+               triag_iter=3, pent_iter=3, hept_iter=3, max_outer_iter=12, extra_iter=5,
+               violated_TriIneq=1e-3, TriIneq=5000, adjust_TriIneq=1, PentIneq=5000, HeptaIneq=5000,
+               Pent_Trials=60, Hepta_Trials=50, include_Pent=1, include_Hepta=1, root=0, use_diff=1,
+               branchingStrategy=1)
+
+
+class Params(C.Structure):
+    _fields_ = PARAM_FIELDS
+
+
+class BabNode(C.Structure):
+    _fields_ = [("xfixed", C.c_int * NMAX), ("sol", C.c_int * NMAX), ("fracsol", C.c_double * NMAX),
+                ("level", C.c_int), ("upper_bound", C.c_double)]
+
+
+class NodeStats(C.Structure):
+    _fields_ = [("bound", C.c_double), ("basic_bound", C.c_double), ("n_sub", C.c_int),
+                ("outer_iters", C.c_int), ("admm_iters", C.c_int), ("ipm_iters", C.c_int),
+                ("n_tri", C.c_int), ("n_pent", C.c_int), ("n_hept", C.c_int),
+                ("pruned", C.c_int), ("gaveup", C.c_int), ("seconds", C.c_double)]
+
+
+def params(**over):
+    p = Params()
+    d = dict(SHIPPED)
+    d.update(over)
+    for k, v in d.items():
+        setattr(p, k, v)
+    return p
+
+
+def node(fixed=None):
+    nd = BabNode()
+    for i, v in (fixed or {}).items():
+        nd.xfixed[i] = 1
+        nd.sol[i] = int(v)
+    return nd
+
+
+class MCBError(RuntimeError):
+    pass
+
+
+_lib = None
+_dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+
+
+def lib():
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise MCBError("libmcbound.so is not built (run madam_gb300.build.build())")
+    L = C.CDLL(LIB_PATH)
+    L.mcb_create.restype = C.c_void_p
+    L.mcb_create.argtypes = [C.POINTER(Params), C.c_int, _dp, C.c_int, C.c_int, C.c_void_p, C.POINTER(C.c_int)]
+    L.mcb_destroy.argtypes = [C.c_void_p]
+    L.mcb_strerror.restype = C.c_char_p
+    L.mcb_strerror.argtypes = [C.c_int]
+    L.mcb_last_error.restype = C.c_char_p
+    L.mcb_last_error.argtypes = [C.c_void_p]
+    L.mcb_set_lb.argtypes = [C.c_void_p, C.c_double, C.c_void_p]
+    L.mcb_get_lb.restype = C.c_double
+    L.mcb_get_lb.argtypes = [C.c_void_p, C.c_void_p]
+    L.mcb_set_diff.argtypes = [C.c_void_p, C.c_double]
+    L.mcb_get_diff.restype = C.c_double
+    L.mcb_get_diff.argtypes = [C.c_void_p]
+    L.mcb_set_trials.argtypes = [C.c_void_p, C.c_int, C.c_int]
+    L.mcb_get_trials.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]
+    L.mcb_evaluate.argtypes = [C.c_void_p, C.POINTER(BabNode), C.c_int, C.POINTER(C.c_double), C.POINTER(NodeStats)]
+    L.mcb_bound_batch.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p]
+    L.mcb_bab.argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_double), C.c_void_p, C.POINTER(C.c_double),
+                          C.POINTER(C.c_int), C.c_void_p, C.c_int, C.POINTER(C.c_int)]
+    L.mcb_op_B.argtypes = [C.c_int, _dp, C.c_int, _ip, C.c_int, _ip, C.c_int, _ip, _dp]
+    L.mcb_op_Bt.argtypes = [C.c_int, _dp, C.c_int, _ip, C.c_int, _ip, C.c_int, _ip, _dp]
+    L.mcb_project_psd.argtypes = [C.c_int, _dp, C.c_int, _dp, _dp, _dp, _dp, C.POINTER(C.c_int)]
+    L.mcb_lambda_max.argtypes = [C.c_int, _dp, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    L.mcb_ipm.argtypes = [C.c_int, _dp, _dp, _dp, _dp, C.POINTER(C.c_double), C.POINTER(C.c_int)]
+    L.mcb_separate_triangles.argtypes = [C.c_int, _dp, C.c_int, C.c_double, _ip, _dp, C.POINTER(C.c_int),
+                                         C.POINTER(C.c_double)]
+    L.mcb_qap_sa_batch.argtypes = [C.c_int, _dp, C.c_int, C.c_int, C.c_uint64, _ip, _dp]
+    L.mcb_kernel_stats.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+    L.mcb_reset_kernel_stats.argtypes = [C.c_void_p]
+    L.mcb_kernel_work.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
+    L.mcb_transfer_stats.argtypes = [C.c_void_p, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]
+    L.mcb_measure_fp64_peak.restype = C.c_double
+    L.mcb_launch_count.restype = C.c_longlong
+    L.mcb_launch_count.argtypes = [C.c_void_p]
+    _lib = L
+    return L
+
+
+def _check(rc, ctx=None):
+    if rc != OK:
+        msg = lib().mcb_strerror(rc).decode()
+        if ctx is not None:
+            extra = lib().mcb_last_error(ctx).decode()
+            if extra:
+                msg += ": " + extra
+        raise MCBError("mcbound error %d (%s)" % (rc, msg))
+
+
+class Context:
+    """A device context for one problem (MADAM's SP and globals)."""
+
+    def __init__(self, prm, SL, N, batch_max=1, flags=PROJ_FP64, stream=None):
+        self.N = N
+        self.SL = np.ascontiguousarray(np.asarray(SL, dtype=np.float64).reshape(-1))
+        st = C.c_int()
+        self.h = lib().mcb_create(C.byref(prm), N, self.SL, batch_max, flags, stream, C.byref(st))
+        if not self.h:
+            _check(st.value)
+        self.batch_max = batch_max
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().mcb_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_lb(self, lb, sol=None):
+        s = None if sol is None else np.ascontiguousarray(sol, dtype=np.int32)
+        lib().mcb_set_lb(self.h, lb, None if s is None else s.ctypes.data)
+        self._keep = s
+
+    def lb(self):
+        s = np.zeros(self.N, dtype=np.int32)
+        v = lib().mcb_get_lb(self.h, s.ctypes.data)
+        return v, s[: self.N - 1]
+
+    def set_diff(self, d):
+        lib().mcb_set_diff(self.h, d)
+
+    def diff(self):
+        return lib().mcb_get_diff(self.h)
+
+    def set_trials(self, p, h):
+        lib().mcb_set_trials(self.h, p, h)
+
+    def trials(self):
+        a, b = C.c_int(), C.c_int()
+        lib().mcb_get_trials(self.h, C.byref(a), C.byref(b))
+        return a.value, b.value
+
+    def evaluate(self, nd, rank=1):
+        b = C.c_double()
+        st = NodeStats()
+        _check(lib().mcb_evaluate(self.h, C.byref(nd), rank, C.byref(b), C.byref(st)), self.h)
+        return b.value, st
+
+    def bound_batch(self, nodes, rank=1):
+        arr = (C.POINTER(BabNode) * len(nodes))(*[C.pointer(nd) for nd in nodes])
+        b = np.zeros(len(nodes))
+        sts = (NodeStats * len(nodes))()
+        _check(lib().mcb_bound_batch(self.h, C.cast(arr, C.c_void_p), len(nodes), rank, b.ctypes.data,
+                                     C.cast(sts, C.c_void_p)), self.h)
+        return b, [sts[i] for i in range(len(nodes))]
+
+    def bab(self, batch=1, max_nodes=0, log_cap=100000):
+        opt, rb = C.c_double(), C.c_double()
+        nodes, lc = C.c_int(), C.c_int()
+        sol = np.zeros(self.N, dtype=np.int32)
+        log = (NodeStats * log_cap)()
+        rc = lib().mcb_bab(self.h, batch, max_nodes, C.byref(opt), sol.ctypes.data, C.byref(rb), C.byref(nodes),
+                           C.cast(log, C.c_void_p), log_cap, C.byref(lc))
+        _check(rc, self.h)
+        return dict(nodes=nodes.value, opt=opt.value, sol=sol[: self.N - 1].copy(), root_bound=rb.value,
+                    log=[log[i] for i in range(lc.value)])
+
+    def kernel_stats(self):
+        cap = 64
+        names = (C.c_char * 32 * cap)()
+        la = (C.c_longlong * cap)()
+        ms = (C.c_double * cap)()
+        k = lib().mcb_kernel_stats(self.h, cap, C.cast(names, C.c_void_p), C.cast(la, C.c_void_p),
+                                   C.cast(ms, C.c_void_p))
+        return {bytes(names[i]).split(b"\0")[0].decode(): (la[i], ms[i]) for i in range(k)}
+
+    def kernel_work(self):
+        cap = 64
+        w = (C.c_double * cap)()
+        u = (C.c_int * cap)()
+        k = lib().mcb_kernel_work(self.h, cap, C.cast(w, C.c_void_p), C.cast(u, C.c_void_p))
+        names = list(self.kernel_stats().keys())
+        return {names[i]: (w[i], u[i]) for i in range(k)}
+
+    def transfer_stats(self):
+        a, b = C.c_longlong(), C.c_longlong()
+        lib().mcb_transfer_stats(self.h, C.byref(a), C.byref(b))
+        return a.value, b.value
+
+    def reset_kernel_stats(self):
+        lib().mcb_reset_kernel_stats(self.h)
+
+    def launch_count(self):
+        return lib().mcb_launch_count(self.h)
+
+
+def fp64_peak_gflops():
+    return lib().mcb_measure_fp64_peak()
+
+
+# ---- operator-level entry points ---------------------------------------------
+def _cuts(tri, pent, hept):
+    t = np.ascontiguousarray(np.asarray(tri, dtype=np.int32).reshape(-1)) if len(tri) else np.zeros(4, np.int32)
+    p = np.ascontiguousarray(np.asarray(pent, dtype=np.int32).reshape(-1)) if len(pent) else np.zeros(6, np.int32)
+    h = np.ascontiguousarray(np.asarray(hept, dtype=np.int32).reshape(-1)) if len(hept) else np.zeros(8, np.int32)
+    return t, len(tri), p, len(pent), h, len(hept)
+
+
+def _fcol(A):
+    return np.ascontiguousarray(np.asarray(A, dtype=np.float64).ravel(order="F"))
+
+
+def op_B(X, tri=(), pent=(), hept=()):
+    n = X.shape[0]
+    t, nt, p, np_, h, nh = _cuts(tri, pent, hept)
+    y = np.zeros(max(nt + np_ + nh, 1))
+    _check(lib().mcb_op_B(n, _fcol(X), nt, t, np_, p, nh, h, y))
+    return y[: nt + np_ + nh]
+
+
+def op_Bt(X, tvec, tri=(), pent=(), hept=()):
+    n = X.shape[0]
+    t, nt, p, np_, h, nh = _cuts(tri, pent, hept)
+    Xf = _fcol(X)
+    tv = np.zeros(max(nt + np_ + nh, 1))
+    tv[: nt + np_ + nh] = tvec
+    _check(lib().mcb_op_Bt(n, Xf, nt, t, np_, p, nh, h, tv))
+    return Xf.reshape(n, n, order="F")
+
+
+def project(W, proj=PROJ_FP64):
+    n = W.shape[0]
+    Xp, Q, Z, ev = np.zeros(n * n), np.zeros(n * n), np.zeros(n * n), np.zeros(n)
+    M = C.c_int()
+    _check(lib().mcb_project_psd(n, _fcol(W), proj, Xp, Q, Z, ev, C.byref(M)))
+    m = M.value
+    return (Xp.reshape(n, n, order="F"), Q.reshape(n, n, order="F"), Z[: n * m].reshape(n, m, order="F"),
+            ev[:m].copy())
+
+
+def lambda_max(A):
+    n = A.shape[0]
+    a, b = C.c_double(), C.c_double()
+    _check(lib().mcb_lambda_max(n, _fcol(A), C.byref(a), C.byref(b)))
+    return a.value, b.value
+
+
+def ipm(L):
+    n = L.shape[0]
+    X, y, Z = np.zeros(n * n), np.zeros(n), np.zeros(n * n)
+    phi, it = C.c_double(), C.c_int()
+    _check(lib().mcb_ipm(n, _fcol(L), X, y, Z, C.byref(phi), C.byref(it)))
+    return it.value, phi.value, X.reshape(n, n, order="F"), y, Z.reshape(n, n, order="F")
+
+
+def sep_triangles(X, K, thr=1e-3):
+    n = X.shape[0]
+    out = np.zeros(4 * K, dtype=np.int32)
+    vals = np.zeros(K)
+    cnt, mv = C.c_int(), C.c_double()
+    _check(lib().mcb_separate_triangles(n, _fcol(X), K, thr, out, vals, C.byref(cnt), C.byref(mv)))
+    return mv.value, out[: 4 * cnt.value].reshape(-1, 4), vals[: cnt.value]
+
+
+def qap_sa_batch(X, k, trials, key):
+    n = X.shape[0]
+    nt = 3 if k == 5 else 4
+    ineq = np.zeros(trials * nt * k, dtype=np.int32)
+    vals = np.zeros(trials * nt)
+    _check(lib().mcb_qap_sa_batch(n, _fcol(X), k, trials, C.c_uint64(key), ineq, vals))
+    return vals, ineq.reshape(-1, k)

@@ -38,6 +38,8 @@ extern "C" {
 #define ORC_MAX_TRI 50000   /* admm.h:34 */
 #define ORC_MAX_PENT 50000  /* admm.h:35 */
 #define ORC_MAX_HEPT 50000  /* admm.h:36 */
+#define ORC_SA_ZERO 1e-11   /* |delta| below this is zero in counter mode */
+#define ORC_SA_MAX_SWEEPS 80 /* sweep cap of the SA in counter mode */
 
 enum { ORC_RNG_GLIBC = 0, ORC_RNG_COUNTER = 1 };
 enum { ORC_TOPK_REFERENCE = 0, ORC_TOPK_CANONICAL = 1 };
@@ -125,6 +127,8 @@ void orc_op_Bt(int n, double *X, int ntri, const int *tri, int npent, const int 
  * Returns M or -1 on LAPACK failure.  canon_sign flips each eigenvector so that its
  * largest-magnitude entry is positive. */
 int orc_project(int n, const double *W, double *Xp, double *Q, double *Z, double *evals, int canon_sign);
+/* dsyevr ABSTOL used by orc_project / orc_lambda_max (default 1e-8 as the reference) */
+void orc_set_abstol(double abstol);
 /* largest eigenvalue as admm.c:731-752 computes it */
 double orc_lambda_max(int n, const double *A);
 /* basic SDP bound by the predictor-corrector IPM (ipm_mc_pk.c); returns iterations or -1 */

@@ -80,6 +80,7 @@ def lib():
     L.orc_op_B.argtypes = [C.c_int, _dp, C.c_int, _ip, C.c_int, _ip, C.c_int, _ip, _dp]
     L.orc_op_Bt.argtypes = [C.c_int, _dp, C.c_int, _ip, C.c_int, _ip, C.c_int, _ip, _dp]
     L.orc_project.argtypes = [C.c_int, _dp, _dp, _dp, _dp, _dp, C.c_int]
+    L.orc_set_abstol.argtypes = [C.c_double]
     L.orc_lambda_max.restype = C.c_double
     L.orc_lambda_max.argtypes = [C.c_int, _dp]
     L.orc_ipm.argtypes = [_dp, C.c_int, _dp, _dp, _dp, C.POINTER(C.c_double)]
@@ -261,8 +262,9 @@ def op_Bt(X, tvec, tri=(), pent=(), hept=()):
     return Xf.reshape(n, n, order="F")
 
 
-def project(W, canon_sign=1):
+def project(W, canon_sign=1, abstol=1e-8):
     n = W.shape[0]
+    lib().orc_set_abstol(abstol)
     Wf = np.asfortranarray(W).ravel(order="F").copy()
     Xp = np.zeros(n * n)
     Q = np.zeros(n * n)
@@ -275,8 +277,9 @@ def project(W, canon_sign=1):
             Z[: n * M].reshape(n, M, order="F"), ev[:M].copy())
 
 
-def lambda_max(A):
+def lambda_max(A, abstol=1e-8):
     n = A.shape[0]
+    lib().orc_set_abstol(abstol)
     return lib().orc_lambda_max(n, np.asfortranarray(A).ravel(order="F").copy())
 
 

@@ -9,6 +9,7 @@
 #include <stdlib.h>
 #include <string.h>
 #include <time.h>
+#include <stdio.h>
 
 #include "orc_internal.h"
 
@@ -245,6 +246,19 @@ static double sdpbound(orc_ctx *c, orc_node *node, int rank, orc_node_stats *st)
         }
         done = prune || giveup || (nbit >= P->ADMM_itermax);
         store_fracsol(c, node);
+        if (getenv("MCB_TRACE")) {
+            uint64_t ht = 1, hp = 1, hh = 1;
+            for (int q = 0; q < 4 * c->ntri; ++q) ht = orc_key2(ht, (uint64_t)c->tri[q]);
+            for (int q = 0; q < 6 * c->npent; ++q) hp = orc_key2(hp, (uint64_t)c->pent[q]);
+            for (int q = 0; q < 8 * c->nhept; ++q) hh = orc_key2(hh, (uint64_t)c->hept[q]);
+            fprintf(stderr, "TRACE round %d nbit %d f %.15g cuts %d %d %d viol3 %.12g viol5 %.12g lb %.1f h %016llx %016llx %016llx\n",
+                    count, nbit, c->f, c->ntri, c->npent, c->nhept, viol3, viol5, c->LB, (unsigned long long)ht,
+                    (unsigned long long)hp, (unsigned long long)hh);
+            if (getenv("MCB_TRACE_SA") && count == atoi(getenv("MCB_TRACE_SA")))
+                for (int q = 0; q < c->npent; ++q)
+                    fprintf(stderr, "PENT %d %d %d %d %d %d\n", c->pent[6 * q], c->pent[6 * q + 1], c->pent[6 * q + 2],
+                            c->pent[6 * q + 3], c->pent[6 * q + 4], c->pent[6 * q + 5]);
+        }
     }
     bound = c->f + fixedvalue;
     if (rank == 0) c->diff = basic_bound - bound;
@@ -270,6 +284,7 @@ END:
 double orc_evaluate(orc_ctx *c, orc_node *node, int rank, orc_node_stats *st) {
     double t0 = now_s();
     orc_set_work_n(c->N);
+    orc_set_abstol(c->rng_mode == ORC_RNG_COUNTER ? 0.0 : 1e-8);
     c->n = orc_create_subproblem(c->N, c->SL, node->xfixed, node->sol, c->L);
     c->node_key = orc_node_key(node->xfixed, node->sol, c->pb);
     double b = sdpbound(c, node, rank, st);

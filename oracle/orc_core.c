@@ -335,6 +335,10 @@ void orc_op_Bt(int n, double *X, int ntri, const int *tri, int npent, const int 
  * unblocked reductions from LWORK, so the size is part of the arithmetic. */
 static int orc_work_n = 0;
 void orc_set_work_n(int N) { orc_work_n = N; }
+/* dsyevr's ABSTOL: the reference passes 1e-8 (operators.c:574, admm.c:738); the
+ * counter (GPU-matching) form asks for full precision (0). */
+static double orc_abstol = 1e-8;
+void orc_set_abstol(double a) { orc_abstol = a; }
 
 int orc_project(int n, const double *W, double *Xp, double *Q, double *Z, double *evals,
                 int canon_sign) {
@@ -353,7 +357,7 @@ int orc_project(int n, const double *W, double *Xp, double *Q, double *Z, double
     VU = ninf < nfro ? ninf : nfro;
     if (VU < VL) VU = 2.0 * VL;
     int IL = 0, IU = 0, M = 0, info = 0;
-    double abstol = 1e-8;
+    double abstol = orc_abstol;
     orc_la.dsyevr("V", "V", "L", &n, A, &n, &VL, &VU, &IL, &IU, &abstol, &M, evals, Z, &n, isuppz,
                   work, &lwork, iwork, &liwork, &info, 1, 1, 1);
     if (info != 0) { /* operators.c:583-593: retry with VL = 0, ABSTOL = 0 */
@@ -405,7 +409,7 @@ double orc_lambda_max(int n, const double *Ain) {
     int *iwork = malloc((size_t)liwork * sizeof(int));
     int *isuppz = malloc((size_t)2 * n * sizeof(int));
     double zdummy[1];
-    double VL = 0, VU = 0, abstol = 1e-8, lam = NAN;
+    double VL = 0, VU = 0, abstol = orc_abstol, lam = NAN;
     int IL = n, IU = n, M = 0, info = 0, ldz = n;
     orc_la.dsyevr("N", "I", "L", &n, A, &n, &VL, &VU, &IL, &IU, &abstol, &M, &lam, zdummy, &ldz,
                   isuppz, work, &lwork, iwork, &liwork, &info, 1, 1, 1);

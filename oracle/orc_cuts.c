@@ -183,9 +183,11 @@ double orc_qap_sa(const int *H, int k, const double *X, int n, int rng_mode, orc
         sol += X[perm[i] + (size_t)perm[i] * n];
         for (int j = i + 1; j < k; ++j) sol += 2 * H[j + i * k] * X[perm[j] + (size_t)perm[i] * n];
     }
-    int not_done = 1;
+    int not_done = 1, sweeps = 0;
     while (not_done > 0) {
         not_done = 0;
+        /* counter mode bounds the sweeps as the GPU build does */
+        if (rng_mode == ORC_RNG_COUNTER && ++sweeps > ORC_SA_MAX_SWEEPS) break;
         for (int it = 0; it < m1; ++it) {
             int i1 = draw_int(&d) % k;
             int i2 = draw_int(&d) % n;
@@ -202,6 +204,10 @@ double orc_qap_sa(const int *H, int k, const double *X, int n, int rng_mode, orc
             double tv2 = 1.0;
             if (i2 < k) tv2 += -2 * H[i1 + k * i2] + 1.0;
             delta += tv1 * tv2;
+            /* Counter mode: a delta that is zero up to rounding noise counts as exactly
+             * zero, so the accept test (and whether it draws) does not depend on the
+             * last bits of X.  glibc mode keeps the reference's behaviour. */
+            if (rng_mode == ORC_RNG_COUNTER && fabs(delta) < ORC_SA_ZERO) delta = 0.0;
             double sol_temp = sol + delta;
             int accept;
             if (delta > 0) {
