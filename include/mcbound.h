@@ -151,6 +151,20 @@ int mcb_op_Bt(int n, double *X, int ntri, const int *tri, int npent, const int *
  * (ascending), evals.  proj = MCB_PROJ_* form. */
 int mcb_project_psd(int n, const double *W, int proj, double *Xp, double *Q, double *Z, double *evals,
                     int *M);
+/* The same projection for callers that cannot allocate device memory (their
+ * memory is handed out by their own pool or capped by their scheduler).  No
+ * counterpart in the reference, which projects host arrays.  W, Xp, Q, Z and
+ * evals are the caller's DEVICE buffers (n*n, n*n, n*n, n*n, n doubles); the
+ * call allocates nothing: its only scratch is a static device array of the
+ * library sized for n <= MCB_NOALLOC_MAX_N (about 2.1 MB on every GPU that
+ * loads the library, for as long as it stays loaded).  Larger n returns
+ * MCB_ERR_ARG.  Runs on `stream` and returns after it completes, with M on the
+ * host.  The first call on a device looks up the scratch's device address
+ * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * Calls share the scratch: calls that overlap on the GPU race. */
+#define MCB_NOALLOC_MAX_N 512
+int mcb_project_psd_noalloc(int n, const double *W, double *Xp, double *Q, double *Z, double *evals, int *M,
+                            void *stream);
 /* largest eigenvalue (admm.c:731-752) and a rigorous upper bound on it */
 int mcb_lambda_max(int n, const double *A, double *lmax, double *lmax_upper);
 /* basic SDP relaxation by the predictor-corrector IPM, ipm_mc_pk.c */

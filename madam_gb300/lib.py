@@ -116,6 +116,8 @@ def lib():
     L.mcb_qap_sa_batch.argtypes = [C.c_int, _dp, C.c_int, C.c_int, C.c_uint64, _ip, _dp]
     L.mcb_kernel_stats.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
     L.mcb_reset_kernel_stats.argtypes = [C.c_void_p]
+    L.mcb_project_psd_noalloc.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                          C.POINTER(C.c_int), C.c_void_p]
     L.mcb_kernel_work.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
     L.mcb_transfer_stats.argtypes = [C.c_void_p, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]
     L.mcb_measure_fp64_peak.restype = C.c_double
@@ -278,6 +280,15 @@ def project(W, proj=PROJ_FP64):
     m = M.value
     return (Xp.reshape(n, n, order="F"), Q.reshape(n, n, order="F"), Z[: n * m].reshape(n, m, order="F"),
             ev[:m].copy())
+
+
+def project_noalloc(n, W_dev, Xp_dev, Q_dev, Z_dev, evals_dev, stream=None):
+    """Allocation-free projection on caller-owned device buffers (pointers as ints)."""
+    M = C.c_int()
+    _check(lib().mcb_project_psd_noalloc(n, C.c_void_p(W_dev), C.c_void_p(Xp_dev), C.c_void_p(Q_dev),
+                                         C.c_void_p(Z_dev), C.c_void_p(evals_dev), C.byref(M),
+                                         None if stream is None else C.c_void_p(stream)))
+    return M.value
 
 
 def lambda_max(A):
