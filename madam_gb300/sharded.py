@@ -1,0 +1,113 @@
+"""Branch-and-bound across ranks: one process per GPU, each with its own node queue.
+
+B&B nodes are independent bound problems, so the tree shards without moving
+matrices: every rank expands the top of the tree identically (the root with
+rank 0 of MADAM's Init_PQ semantics, then `depth` levels by the reference's
+most-fractional rule), deals the frontier round-robin, and runs its own
+best-first search.  The only exchange is the incumbent: a max-allreduce of the
+lower bound after every batch (MADAM pushes NEW_VALUE to its master,
+bab_functions.c:242-256), plus a sum-allreduce of queue sizes to detect global
+termination.  No matrix data crosses ranks, so there is no device collective.
+
+`ctx` is any object with evaluate(node, rank) -> (bound, stats), set_lb(lb, sol),
+lb() -> (lb, sol) and an `N` attribute; `new_node(fixed)` builds a node with
+xfixed / sol / fracsol arrays (the BabNode layout).
+"""
+import heapq
+import itertools
+
+import numpy as np
+
+
+def _branch_var(nd, pb, strategy=1):
+    best, ic = (1e9 if strategy == 1 else -1e9), -1
+    for i in range(pb):
+        if nd.xfixed[i]:
+            continue
+        v = abs(0.5 - nd.fracsol[i])
+        if (strategy == 1 and v < best) or (strategy == 0 and v > best):
+            best, ic = v, i
+    return ic
+
+
+def _fixed(nd, pb):
+    return {i: int(nd.sol[i]) for i in range(pb) if nd.xfixed[i]}
+
+
+def sharded_bab(ctx, new_node, dist=None, depth=2, max_nodes=100000):
+    """Returns (optimum, solution vector, nodes evaluated on this rank, evaluated on all ranks)."""
+    rank = dist.get_rank() if dist else 0
+    world = dist.get_world_size() if dist else 1
+    pb = ctx.N - 1
+
+    def allreduce(v, op):
+        if not dist:
+            return v
+        import torch
+
+        t = torch.tensor([v], dtype=torch.float64)
+        dist.all_reduce(t, op=op)
+        return float(t[0])
+
+    MAX = dist.ReduceOp.MAX if dist else None
+    SUM = dist.ReduceOp.SUM if dist else None
+    # every rank expands the top of the tree identically: the root with rank 0
+    # semantics (Init_PQ), branched at once as MADAM's master does (main.c:126-158);
+    # `depth` - 1 further levels are bounded redundantly on every rank
+    root = new_node({})
+    rb, _ = ctx.evaluate(root, 0)
+    evaluated = 1
+    frontier = []  # unevaluated nodes: (parent bound, fixings)
+
+    def children(b, fx, nd):
+        ic = _branch_var(nd, pb)
+        out = []
+        if ic >= 0 and ctx.lb()[0] + 1.0 < b:
+            for v in (0, 1):
+                f2 = dict(fx)
+                f2[ic] = v
+                out.append((b, f2))
+        return out
+
+    frontier = children(rb, {}, root)
+    for _ in range(depth - 1):
+        nxt = []
+        for b, fx in frontier:
+            nd = new_node(fx)
+            cb, _ = ctx.evaluate(nd, 1)
+            evaluated += 1
+            nxt += children(cb, fx, nd)
+        frontier = nxt
+    lb, sol = ctx.lb()
+    # deal the frontier; each rank keeps a best-first heap keyed on the bound
+    mine = [f for k, f in enumerate(sorted(frontier, key=lambda t: sorted(t[1].items()))) if k % world == rank]
+    tie = itertools.count()
+    heap = [(-b, next(tie), fx, new_node(fx)) for b, fx in mine]
+    heapq.heapify(heap)
+    local = 0
+    while True:
+        g = allreduce(lb, MAX)
+        if g > lb:
+            lb = g
+            ctx.set_lb(lb, None)
+        active = allreduce(float(len(heap)), SUM)
+        if active == 0 or local >= max_nodes:
+            break
+        if heap:
+            negb, _, fx, nd = heapq.heappop(heap)
+            if lb + 1.0 < -negb:
+                b, _ = ctx.evaluate(nd, 1)
+                local += 1
+                lb2, sol2 = ctx.lb()
+                if lb2 > lb:
+                    lb, sol = lb2, sol2
+                if lb + 1.0 < b:
+                    ic = _branch_var(nd, pb)
+                    for v in (0, 1):
+                        f2 = dict(fx)
+                        f2[ic] = v
+                        heapq.heappush(heap, (-b, next(tie), f2, new_node(f2)))
+    best = allreduce(lb, MAX)
+    total = allreduce(float(local + evaluated), SUM)
+    own = np.asarray(sol)[:pb] if lb == best else None
+    return best, own, local + evaluated, int(total)

@@ -1,0 +1,133 @@
+"""CPU tests of the host side: graph construction, the C ABI surface of the
+built library (symbols only, no device calls), parameter layout, the benchmark's
+reference arm and the sharded multi-rank driver on gloo."""
+import json
+import os
+import re
+import subprocess
+import sys
+
+import numpy as np
+import pytest
+
+from madam_gb300 import graphs as G
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+REF = "/root/reference"
+
+
+def test_extended_laplacian_matches_oracle(orc):
+    for seed, wts in ((1, "one"), (2, "pm1"), (3, "int10")):
+        n, e, w = G.gnp(30, 0.4, wts, seed=seed)
+        assert np.array_equal(G.extended_laplacian(n, e, w).ravel(order="F"), orc.build_L(n, (e, w)))
+
+
+def test_rudy_roundtrip(tmp_path):
+    n, e, w = G.gnp(20, 0.5, "int10", seed=4)
+    f = tmp_path / "g.rudy"
+    G.write_rudy(str(f), n, e, w)
+    n2, e2, w2 = G.read_rudy(str(f))
+    assert n2 == n and np.array_equal(e2, e) and np.array_equal(w2, w)
+
+
+def test_torus_is_4_regular():
+    n, e, w = G.torus2d(5, 6, seed=1)
+    deg = np.bincount(np.asarray(e).ravel() - 1, minlength=n)
+    assert n == 30 and np.all(deg == 4) and set(np.unique(w)) <= {-1.0, 1.0}
+
+
+def test_c_abi_library_exports_every_declared_symbol():
+    from madam_gb300 import build as B
+
+    lib = B.build()
+    hdr = open(os.path.join(ROOT, "include", "mcbound.h")).read()
+    declared = set(re.findall(r"\b(mcb_[a-z_0-9]+)\s*\(", hdr))
+    out = subprocess.run(["nm", "-D", "--defined-only", lib], capture_output=True, text=True).stdout
+    exported = set(re.findall(r" T (mcb_[a-z_0-9]+)$", out, re.M))
+    assert declared, "no declarations parsed"
+    assert declared <= exported, declared - exported
+
+
+def test_library_loads_without_a_device():
+    import ctypes
+
+    from madam_gb300 import build as B
+
+    L = ctypes.CDLL(B.build())
+    L.mcb_strerror.restype = ctypes.c_char_p
+    assert L.mcb_version() >= 10000
+    assert L.mcb_strerror(-5) == b"capacity exceeded"
+
+
+def test_params_and_node_layout_match_the_reference():
+    from madam_gb300 import lib as M
+
+    names = [f[0] for f in M.PARAM_FIELDS]
+    if os.path.isdir(REF):
+        txt = open(os.path.join(REF, "admm.h")).read()
+        ref = re.findall(r"P\((?:double|int),\s*(\w+),", txt)
+        assert names == ref
+    import ctypes
+
+    assert ctypes.sizeof(M.BabNode) == 4 * 1024 * 2 + 8 * 1024 + 8 + 8
+    assert M.BabNode.upper_bound.offset == 4 * 1024 * 2 + 8 * 1024 + 8
+
+
+def test_workload_is_deterministic():
+    from madam_gb300 import workload as W
+
+    a, b = W.make("gnp100_one_tri"), W.make("gnp100_one_tri")
+    assert np.array_equal(a["SL"], b["SL"]) and a["fixings"] == b["fixings"] and a["lb"] == b["lb"]
+    assert G.cut_value(a["n"], a["edges"], a["weights"], a["lb_sol"]) == a["lb"]
+
+
+def test_bench_reference_arm_prints_one_json_line():
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--workload",
+                        "gnp100_one_tri", "--steps", "1", "--warmup", "0", "--cpu-sample", "2"],
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    line = json.loads(r.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["value"] > 0 and line["unit"] == "nodes/s"
+    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["cpu_baseline"]["kind"] == "port"
+
+
+def _sharded_worker(rank, world, port, q):
+    import torch.distributed as dist
+
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    sys.path.insert(0, ROOT)
+    from madam_gb300 import graphs as G2
+    from madam_gb300.sharded import sharded_bab
+    from oracle import oracle as O
+
+    n, e, w = G2.gnp(64, 0.5, "pm1", seed=13)
+    SL = O.build_L(n, (e, w))
+    ctx = O.Ctx(O.shipped_params(), SL, n)
+    best, sol, mine, total = sharded_bab(ctx, lambda fx: O.make_node(n - 1, fx), dist=dist, depth=2)
+    q.put((rank, best, mine, total, None if sol is None else G2.cut_value(n, e, w, sol)))
+    dist.destroy_process_group()
+
+
+def test_sharded_branch_and_bound_on_two_gloo_ranks(orc):
+    import torch.multiprocessing as mp
+
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = 29500 + os.getpid() % 1000
+    ps = [ctx.Process(target=_sharded_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in ps:
+        p.start()
+    res = [q.get(timeout=600) for _ in ps]
+    for p in ps:
+        p.join(timeout=60)
+    # single-process reference answer (oracle, same counter streams)
+    n, e, w = G.gnp(64, 0.5, "pm1", seed=13)
+    SL = orc.build_L(n, (e, w))
+    c = orc.Ctx(orc.shipped_params(), SL, n)
+    serial = c.bab(max_nodes=5000)
+    bests = {r[1] for r in res}
+    assert bests == {serial["opt"]}
+    assert any(r[4] == serial["opt"] for r in res)
+    assert res[0][3] == res[1][3]

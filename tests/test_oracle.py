@@ -1,0 +1,181 @@
+"""CPU checks of the oracle itself: against glibc, against fixtures produced by
+the reference (compiled from its own sources), against the reference's
+published outputs, and against independent numpy restatements."""
+import ctypes
+import glob
+import json
+import os
+import re
+
+import numpy as np
+import pytest
+
+from madam_gb300 import graphs as G
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF = "/root/reference"
+
+
+def test_glibc_rand_restatement_matches_libc(orc):
+    libc = ctypes.CDLL("libc.so.6")
+    for seed in (2020, 1, 12345):
+        libc.srand(seed)
+        ref = [libc.rand() for _ in range(3000)]
+        assert orc.glibc_stream(seed, 3000) == ref
+
+
+def _fixture_instance(f):
+    if f["kind"] == "gnp":
+        n, p, w, seed = f["args"]
+        return G.gnp(n, p, w, seed=seed)
+    return G.torus2d(f["args"][0], f["args"][1], seed=f["args"][2])
+
+
+FIXTURES = json.load(open(os.path.join(HERE, "golden", "reference_bab.json")))["instances"]
+
+
+@pytest.mark.parametrize("fx", FIXTURES, ids=[f["name"] for f in FIXTURES])
+def test_oracle_reproduces_reference_branch_and_bound(orc, fx):
+    """Whole B&B trees of the reference (strict-IEEE build), node by node."""
+    n, e, w = _fixture_instance(fx)
+    SL = orc.build_L(n, (e, w))
+    c = orc.Ctx(orc.shipped_params(), SL, n, rng=orc.RNG_GLIBC, topk=orc.TOPK_REFERENCE, canon_sign=0)
+    r = c.bab(max_nodes=2000)
+    bounds = [s.bound for s in r["log"]]
+    assert r["nodes"] == fx["nodes"]
+    assert r["opt"] == fx["opt"]
+    assert sorted(np.nonzero(r["sol"])[0].tolist()) == sorted(fx["sol"])
+    assert len(bounds) == len(fx["bounds"])
+    # the reference prints 12 decimals
+    assert max(abs(a - b) for a, b in zip(bounds, fx["bounds"])) <= 1e-9
+
+
+def test_oracle_counter_mode_is_order_free(orc):
+    """Counter streams: a node's bound does not depend on what was bounded before."""
+    n, e, w = G.gnp(36, 0.5, "pm1", seed=21)
+    SL = orc.build_L(n, (e, w))
+    prm = orc.shipped_params(use_diff=0)
+    a = orc.Ctx(prm, SL, n)
+    b = orc.Ctx(prm, SL, n)
+    a.set_lb(0)
+    b.set_lb(0)
+    a.evaluate(orc.make_node(n - 1, {4: 1}), rank=1)
+    a.set_lb(0)
+    ba, _ = a.evaluate(orc.make_node(n - 1, {2: 0}), rank=1)
+    bb, _ = b.evaluate(orc.make_node(n - 1, {2: 0}), rank=1)
+    assert ba == bb
+
+
+def _published():
+    out = []
+    for f in sorted(glob.glob(os.path.join(REF, "Instances/rudy/rudy_150/*/*.output"))):
+        txt = open(f).read()
+        opt = float(re.search(r"^Maximum value = (\S+)", txt, re.M).group(1))
+        root = float(re.search(r"^Root node bound = (\S+)", txt, re.M).group(1))
+        sol = [int(v) for v in re.search(r"^Solution = \( (.*)\)", txt, re.M).group(1).split()]
+        sigma0 = float(re.search(r"sigma0 = (\S+)", txt).group(1))
+        out.append((f[: -len(".output")], opt, root, sol, sigma0))
+    return out
+
+
+@pytest.mark.skipif(not os.path.isdir(REF), reason="reference instances not present")
+def test_published_optima_are_cut_values_of_published_solutions():
+    pubs = _published()
+    assert len(pubs) == 90
+    for inst, opt, _, sol, _ in pubs:
+        n, e, w = G.read_rudy(inst)
+        side = np.zeros(n, dtype=np.int32)
+        side[np.array(sol) - 1] = 1
+        assert G.cut_value(n, e, w, side) == opt
+        # the published optimum is also what the extended Laplacian evaluates to
+        L = G.extended_laplacian(n, e, w)
+        x = side[: n - 1].astype(float)
+        assert abs(x @ L[: n - 1, : n - 1] @ x - opt) < 1e-6
+
+
+@pytest.mark.slow
+@pytest.mark.skipif(not os.path.isdir(REF), reason="reference instances not present")
+def test_oracle_root_bounds_near_published(orc):
+    """The published root bounds came from a -ffast-math build whose k-gonal SA
+    path depends on rounding noise; the oracle lands within 0.1%."""
+    for inst, opt, root, _, sigma0 in _published()[:2]:
+        n, e, w = G.read_rudy(inst)
+        SL = orc.build_L(n, (e, w))
+        c = orc.Ctx(orc.shipped_params(sigma0=sigma0, root=1), SL, n, rng=orc.RNG_GLIBC, topk=orc.TOPK_REFERENCE,
+                    canon_sign=0)
+        b, _ = c.evaluate(orc.make_node(n - 1), rank=0)
+        assert b >= opt
+        assert abs(b - root) <= 1e-3 * root
+
+
+# ---- numpy restatements of the operators ------------------------------------
+def _np_op_B(X, tri, pent, hept):
+    y = []
+    for (i, j, k, t) in tri:
+        e = {1: (1, 1, 1), 2: (1, 1, -1), 3: (1, -1, 1), 4: (-1, 1, 1)}[t]
+        p = (i, j, k)
+        y.append(-sum(e[a] * e[b] * X[max(p[a], p[b]), min(p[a], p[b])] for a in range(3) for b in range(a + 1, 3)))
+    for c in list(pent) + list(hept):
+        t, p = c[0], c[1:]
+        k = len(p)
+        e = [-1 if a < t - 1 else 1 for a in range(k)]
+        s = {5: 0.5, 7: 1.0 / 3.0}[k]
+        y.append(-s * sum(e[a] * e[b] * X[max(p[a], p[b]), min(p[a], p[b])] for a in range(k) for b in range(a + 1, k)))
+    return np.array(y)
+
+
+def test_oracle_operators_against_numpy(orc):
+    rng = np.random.default_rng(5)
+    n = 20
+    X = rng.standard_normal((n, n))
+    X = X + X.T
+    tri = [tuple(sorted(rng.choice(n, 3, replace=False))[::-1]) + (int(rng.integers(1, 5)),) for _ in range(15)]
+    pent = [(int(rng.integers(1, 4)),) + tuple(int(v) for v in rng.choice(n, 5, replace=False)) for _ in range(6)]
+    hept = [(int(rng.integers(1, 5)),) + tuple(int(v) for v in rng.choice(n, 7, replace=False)) for _ in range(6)]
+    assert np.allclose(orc.op_B(X, tri, pent, hept), _np_op_B(X, tri, pent, hept), atol=1e-12)
+    # adjoint: <B^T t, X> = <t, B(X)> with the Frobenius product on symmetric matrices
+    t = rng.standard_normal(len(tri) + len(pent) + len(hept))
+    BtT = -(orc.op_Bt(np.zeros((n, n)), t, tri, pent, hept))
+    Y = np.tril(X) + np.tril(X, -1).T
+    assert abs(np.sum(BtT * Y) - t @ orc.op_B(Y, tri, pent, hept)) < 1e-10
+
+
+def test_oracle_projection_against_numpy(orc):
+    rng = np.random.default_rng(3)
+    n = 40
+    A = rng.standard_normal((n, n))
+    W = A + A.T
+    Xp, Q, Z, ev = orc.project(W, abstol=0.0)
+    w, V = np.linalg.eigh(W)
+    Xr = (V[:, w > 1e-8] * w[w > 1e-8]) @ V[:, w > 1e-8].T
+    assert np.allclose(np.tril(Xp), np.tril(Xr), atol=1e-12)
+    assert np.allclose(Z @ Z.T, Xr, atol=1e-12)
+    assert np.allclose(np.tril(Q), np.tril(Xr - W), atol=1e-12)
+    assert np.all(np.triu(Q, 1) == 0.0)
+
+
+def test_create_subproblem_against_numpy(orc):
+    n, e, w = G.gnp(25, 0.5, "int10", seed=9)
+    SL = G.extended_laplacian(n, e, w)
+    fixed = {3: 1, 7: 0, 10: 1}
+    xf = np.zeros(n, np.int32)
+    so = np.zeros(n, np.int32)
+    for i, v in fixed.items():
+        xf[i], so[i] = 1, v
+    m, PL = orc.create_subproblem(SL.ravel(order="F"), n, xf, so)
+    U = [i for i in range(n - 1) if not xf[i]]
+    F1 = [i for i in range(n - 1) if xf[i] and so[i] == 1]
+    Lap = SL[: n - 1, : n - 1]
+    B = Lap[np.ix_(U, U)]
+    fr = Lap[np.ix_(U, F1)].sum(axis=1)
+    rs = B.sum(axis=1) + 2 * fr
+    ref = np.zeros((m, m))
+    ref[: m - 1, : m - 1] = B + np.diag(2 * fr)
+    ref[m - 1, : m - 1] = rs
+    ref[: m - 1, m - 1] = rs
+    ref[m - 1, m - 1] = rs.sum()
+    assert m == len(U) + 1
+    assert np.allclose(PL, 0.25 * ref, atol=1e-12)
+    fv = orc.fixed_value(SL.ravel(order="F"), n, xf, so)
+    x = np.array([so[i] if xf[i] else 0 for i in range(n - 1)], float)
+    assert abs(fv - x @ Lap @ x) < 1e-9
