@@ -48,6 +48,10 @@ enum mcb_status {
 #define MCB_PROJ_NS_TF32 0x2   /* chosen: TF32 Newton-Schulz sign iteration + FP64 refinement */
 /* Other flags */
 #define MCB_FLAG_PROFILE 0x100 /* time every kernel class with CUDA events */
+/* operands of the Newton-Schulz growth steps (mcb_ns_options) */
+#define MCB_NS_OPERANDS_NATIVE 0 /* one pass of the form's type (BF16 / TF32): rounding floor ~1e-3 */
+#define MCB_NS_OPERANDS_SPLIT 1  /* FP32-accurate: each operand split into three BF16 pieces (default) */
+#define MCB_NS_OPERANDS_FP32 2   /* FP32 FMA, no tensor cores (reference point) */
 #define MCB_FLAG_LEARNED 0x200 /* learned cut ranking + dual warm start (needs mcb_load_model) */
 
 /* Same fields, order and meaning as MADAM's Parameters (admm.h:57-89). */
@@ -120,6 +124,14 @@ void mcb_set_diff(mcb_ctx *ctx, double diff);
 double mcb_get_diff(const mcb_ctx *ctx);
 void mcb_set_trials(mcb_ctx *ctx, int pent_trials, int hepta_trials);
 void mcb_get_trials(const mcb_ctx *ctx, int *pent_trials, int *hepta_trials);
+/* Newton-Schulz forms only (no counterpart in the reference, whose projection is
+ * dsyevr): growth-step operands (MCB_NS_OPERANDS_*) and l0, the smallest
+ * |eigenvalue| / ||W||_F the sign iteration resolves (default 1e-6; smaller
+ * eigenvalues change X+ by at most l0 ||W||_F / 2 each).  MCB_ERR_ARG on the FP64 form. */
+int mcb_ns_options(mcb_ctx *ctx, int operands, double l0);
+/* the Newton-Schulz step schedule of the context: count, and per step a, b of
+ * S <- a S + b S^3 and whether its operands are FP32-accurate */
+int mcb_ns_schedule(const mcb_ctx *ctx, int cap, float *a, float *b, int *accurate);
 
 /* ---- the bound ---------------------------------------------------------------
  * mcb_evaluate: Evaluate(node, SP, PP, rank) (evaluate.c:12).  Writes
@@ -148,7 +160,10 @@ int mcb_op_Bt(int n, double *X, int ntri, const int *tri, int npent, const int *
               const int *hept, const double *t);
 /* PSD projection, operators.c:521-619: W (lower) -> Xp = W_+ (full symmetric),
  * Q = Xp - W (lower), Z = eigenvectors * sqrt(lambda) of the M eigenvalues > 1e-8
- * (ascending), evals.  proj = MCB_PROJ_* form. */
+ * (ascending), evals.  proj = MCB_PROJ_* form; the Newton-Schulz forms may add
+ * MCB_PROJ_OPERANDS(MCB_NS_OPERANDS_*) and write neither Z nor evals (M is the
+ * rounded (n + trace sign(W)) / 2). */
+#define MCB_PROJ_OPERANDS(op) (((op) + 1) << 4)
 int mcb_project_psd(int n, const double *W, int proj, double *Xp, double *Q, double *Z, double *evals,
                     int *M);
 /* The same projection for callers that cannot allocate device memory (their

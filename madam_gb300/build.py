@@ -52,7 +52,7 @@ def build(force=False, verbose=False):
             if w:
                 sys.stderr.write(w)
     if not os.path.exists(LIB) or any(os.path.getmtime(o) > os.path.getmtime(LIB) for o in objs):
-        cmd = [NVCC] + ARCH + ["-shared", "-o", LIB] + objs
+        cmd = [NVCC] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcublas"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed:\n%s%s" % (r.stdout, r.stderr))

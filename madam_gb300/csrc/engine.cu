@@ -24,6 +24,7 @@
 #include "host_cuts.h"
 #include "kernels.h"
 #include "mcb_dev.cuh"
+#include "ns.h"
 
 using namespace mcb;
 
@@ -31,11 +32,13 @@ namespace {
 
 const char *kClassNames[] = {"subproblem", "ipm",   "admm_rhs", "cg",        "admm_su", "build_W",
                              "sym_copy",   "tridiag", "bisect", "invit",     "backtrans", "canon_scale",
-                             "syrk_post",  "admm_bx", "admm_finish", "safe_bound", "tri_sep", "sa"};
-// unit of mcb_ctx::work per class: 1 = FP64 flops, 2 = bytes, 0 = not counted
-const int kWorkUnit[] = {0, 0, 2, 0, 0, 2, 2, 1, 0, 0, 1, 0, 1, 0, 0, 0, 0, 0};
+                             "syrk_post",  "admm_bx", "admm_finish", "safe_bound", "tri_sep", "sa",
+                             "ns_prep",    "ns_gemm", "ns_fp64", "heur_gpu"};
+// unit of mcb_ctx::work per class: 1 = FP64 flops, 2 = bytes, 3 = tensor-core GEMM
+// flops (the Newton-Schulz steps, low-precision and FP32-accurate), 0 = not counted
+const int kWorkUnit[] = {0, 0, 2, 0, 0, 2, 2, 1, 0, 0, 1, 0, 1, 0, 0, 0, 0, 0, 2, 3, 1, 0};
 enum KClass { K_SUB, K_IPM, K_RHS, K_CG, K_SU, K_W, K_SYMC, K_TRID, K_BIS, K_INV, K_BACK, K_CANON, K_SYRK,
-              K_BX, K_FIN, K_SAFE, K_TRI, K_SA, K_NCLASS };
+              K_BX, K_FIN, K_SAFE, K_TRI, K_SA, K_NSPREP, K_NSGEMM, K_NSREF, K_HEUR, K_NCLASS };
 
 struct DevBuf {
     void *p = nullptr;
@@ -69,6 +72,7 @@ struct NodeRun : CutLists {
     std::vector<double> tri_y, pent_y, hept_y;
     std::vector<double> Lsub;          // n x n subproblem matrix (host copy for the heuristic)
     std::vector<double> Zf;            // n x M factor of the last projection (times sqrt(sigma))
+    std::vector<unsigned char> signs;  // Newton-Schulz form: hyperplane signs (n x N, 1 = negative)
     std::vector<int> x;                // heuristic result (BabPbSize)
     double hval = -kBig;
 };
@@ -105,6 +109,12 @@ struct mcb_ctx {
     int *d_perm = nullptr, *d_saout = nullptr;
     double *d_saval = nullptr;
     size_t sa_cap = 0;
+    // Newton-Schulz projection (chosen form)
+    int proj = MCB_PROJ_FP64;
+    NsProj ns;
+    int *d_hlist = nullptr;
+    unsigned long long *d_hkeys = nullptr;
+    unsigned char *d_hsign = nullptr;
     // instrumentation
     long long h2d = 0, d2h = 0;        // host<->device bytes moved by the bound calls
     double work[K_NCLASS] = {};        // algorithmic work per class (flops or bytes, see kWorkUnit)
@@ -331,17 +341,44 @@ void launch_projection(mcb_ctx *c, int ns, int gate) {
     { Prof p(c, K_CANON, 1); launch_canon_scale(d, ns, N, gate, c->st); }
 }
 
-void launch_admm_iteration(mcb_ctx *c, int ns, int mmax, int emax) {
+// the Newton-Schulz projection of every live slot, X+ into the ADMM epilogue
+int launch_ns_projection(mcb_ctx *c, int ns) {
+    Slot *d = c->d_slots;
+    NsProj &P = c->ns;
+    { Prof p(c, K_NSPREP, 2); launch_ns_prep(d, ns, P.npad, P.stride, P.S, P.Wd, 1, c->st); }
+    double lo = P.flops_lo, hi = P.flops_hi, f64 = P.flops_fp64;
+    int rc;
+    {
+        Prof p(c, K_NSGEMM, 3 * (int)P.steps.size() + 1);
+        rc = P.sign(d, ns, 1, c->st);
+    }
+    if (rc) return set_err(c, rc, "cuBLAS GEMM of the Newton-Schulz step failed");
+    { Prof p(c, K_NSREF, 1); rc = P.product(c->st); }
+    if (rc) return set_err(c, rc, "cuBLAS FP64 GEMM of the projection failed");
+    c->work[K_NSGEMM] += (P.flops_lo - lo) + (P.flops_hi - hi);
+    c->work[K_NSREF] += P.flops_fp64 - f64;
+    c->work[K_NSPREP] += 8.0 * (double)P.live * P.npad * P.npad * 2.5;
+    { Prof p(c, K_SYRK, 2); launch_ns_post(d, ns, c->N, c->d_partials, P.Gd, P.npad, P.stride, c->st); }
+    return MCB_OK;
+}
+
+int launch_admm_iteration(mcb_ctx *c, int ns, int mmax, int emax) {
     Slot *d = c->d_slots;
     int N = c->N;
     { Prof p(c, K_RHS, 1); launch_admm_rhs(d, ns, N, mmax, c->st); }
     { Prof p(c, K_CG, 1); launch_cg(d, ns, 2000, c->st); }
     { Prof p(c, K_SU, 1); launch_admm_su(d, ns, mmax, c->st); }
     { Prof p(c, K_W, 2); launch_build_W(d, ns, N, emax, 0, c->st); }
-    launch_projection(c, ns, 1);
-    { Prof p(c, K_SYRK, 2); launch_syrk_post(d, ns, N, 1, c->d_partials, c->st); }
+    if (c->proj == MCB_PROJ_FP64) {
+        launch_projection(c, ns, 1);
+        { Prof p(c, K_SYRK, 2); launch_syrk_post(d, ns, N, 1, c->d_partials, c->st); }
+    } else {
+        int rc = launch_ns_projection(c, ns);
+        if (rc) return rc;
+    }
     { Prof p(c, K_BX, 1); launch_admm_bx(d, ns, mmax, c->st); }
     { Prof p(c, K_FIN, 1); launch_admm_finish(d, ns, c->prm.scaleSigma, c->prm.ADMM_itermax, c->st); }
+    return MCB_OK;
 }
 
 // --- heuristic (heuristic.c), counter streams --------------------------------
@@ -398,11 +435,17 @@ void run_heuristic(const mcb_ctx *c, NodeRun &r) {
         Stream st;
         st.key = key2(key2(r.key, 0x48455552ull + (uint64_t)r.heur_calls), (uint64_t)count);
         st.ctr = 0;
-        for (int i = 0; i < M; ++i) v[i] = st.next_unit() - 0.5;
-        for (int i = 0; i < N; ++i) {
-            double sca = 0.0;
-            for (int j = 0; j < M; ++j) sca += v[j] * r.Zf[(size_t)j * N + i];
-            tx[i] = sca < 0 ? -1 : 1;
+        if (!r.signs.empty()) {
+            // Newton-Schulz form: signs of X v computed on the GPU
+            const unsigned char *sg = &r.signs[(size_t)count * N];
+            for (int i = 0; i < N; ++i) tx[i] = sg[i] ? -1 : 1;
+        } else {
+            for (int i = 0; i < M; ++i) v[i] = st.next_unit() - 0.5;
+            for (int i = 0; i < N; ++i) {
+                double sca = 0.0;
+                for (int j = 0; j < M; ++j) sca += v[j] * r.Zf[(size_t)j * N + i];
+                tx[i] = sca < 0 ? -1 : 1;
+            }
         }
         mc_1opt(tx.data(), r.Lsub.data(), N, Lx, d, delta, I);
         int index = 0;
@@ -676,6 +719,42 @@ uint64_t node_key(const int *xfixed, const int *sol, int pb) {
     return h;
 }
 
+// Newton-Schulz form: the heuristic's hyperplane signs sign(X v) for every node in
+// hrun, computed on the GPU (one TF32 GEMM per node) and copied to r.signs
+int ns_hyperplanes(mcb_ctx *c, std::vector<NodeRun *> &runs, std::vector<NodeRun *> &hrun) {
+    std::vector<int> list;
+    std::vector<unsigned long long> keys;
+    int nm = 1;
+    for (size_t q = 0; q < hrun.size(); ++q) {
+        NodeRun *r = hrun[q];
+        int si = -1;
+        for (size_t k = 0; k < runs.size(); ++k)
+            if (runs[k] == r) si = (int)k;
+        if (r->M == 0) { r->signs.clear(); continue; }  // X+ = 0: all-ones start, as the plain form
+        list.push_back(si);
+        keys.push_back(key2(r->key, 0x48455552ull + (uint64_t)r->heur_calls));
+        nm = std::max(nm, r->n);
+    }
+    if (list.empty()) return MCB_OK;
+    const int count = c->N, k = (int)list.size();
+    const size_t ostride = (size_t)c->N * c->N;
+    CUDA_TRY(c, h2d(c, c->d_hlist, list.data(), k * sizeof(int)));
+    CUDA_TRY(c, h2d(c, c->d_hkeys, keys.data(), k * sizeof(unsigned long long)));
+    int rc;
+    {
+        Prof p(c, K_HEUR, 4);
+        rc = c->ns.hyperplanes(c->d_slots, list, c->d_hlist, c->d_hkeys, count, (nm + 15) / 16 * 16, c->d_hsign,
+                               ostride, c->st);
+    }
+    if (rc) return set_err(c, rc, "hyperplane GEMM failed");
+    for (int q = 0; q < k; ++q) {
+        NodeRun &r = *runs[list[q]];
+        r.signs.resize((size_t)r.n * count);
+        CUDA_TRY(c, d2h(c, r.signs.data(), c->d_hsign + (size_t)q * ostride, r.signs.size()));
+    }
+    return MCB_OK;
+}
+
 // --- the batched SDPbound ----------------------------------------------------
 int bound_batch(mcb_ctx *c, mcb_bab_node *const *nodes, int count, int rank, double *bounds, mcb_node_stats *stats) {
     auto t0 = std::chrono::steady_clock::now();
@@ -791,7 +870,15 @@ int bound_batch(mcb_ctx *c, mcb_bab_node *const *nodes, int count, int rank, dou
             const int chunk = 8;
             std::vector<int> nb0(ns);
             for (int si = 0; si < ns; ++si) nb0[si] = c->hs[si].nbit;
-            for (int k = 0; k < chunk; ++k) launch_admm_iteration(c, ns, mmax, emax);
+            if (c->proj != MCB_PROJ_FP64) {
+                std::vector<int> lv;
+                int nm = 1;
+                for (int si = 0; si < ns; ++si)
+                    if (live[si] && !c->hs[si].stop) { lv.push_back(si); nm = std::max(nm, c->hs[si].n); }
+                if ((rc = c->ns.set_live(lv, (nm + 15) / 16 * 16, c->st))) return set_err(c, rc, "pointer upload");
+            }
+            for (int k = 0; k < chunk; ++k)
+                if ((rc = launch_admm_iteration(c, ns, mmax, emax))) return rc;
             it += chunk;
             if ((rc = download_slots(c, ns))) return rc;
             for (int si = 0; si < ns; ++si) {
@@ -841,16 +928,20 @@ int bound_batch(mcb_ctx *c, mcb_bab_node *const *nodes, int count, int rank, dou
             r.bound = r.f + r.fixedvalue;
             r.prune = r.bound < c->LB + 1.0;
             if (!r.prune) {
-                double sg = acc[(size_t)si * kAcc + ACC_SIGMA_LAST];
-                r.Zf.resize((size_t)r.n * r.M);
-                if (r.M > 0) {
-                    CUDA_TRY(c, d2h(c, r.Zf.data(), s.V, r.Zf.size() * sizeof(double)));
-                    double sca = sqrt(sg);
-                    for (auto &z : r.Zf) z *= sca;
+                if (c->proj == MCB_PROJ_FP64) {
+                    double sg = acc[(size_t)si * kAcc + ACC_SIGMA_LAST];
+                    r.Zf.resize((size_t)r.n * r.M);
+                    if (r.M > 0) {
+                        CUDA_TRY(c, d2h(c, r.Zf.data(), s.V, r.Zf.size() * sizeof(double)));
+                        double sca = sqrt(sg);
+                        for (auto &z : r.Zf) z *= sca;
+                    }
                 }
                 hrun.push_back(&r);
             }
         }
+        if (c->proj != MCB_PROJ_FP64 && !hrun.empty())
+            if ((rc = ns_hyperplanes(c, runs, hrun))) return rc;
         run_heuristics(c, hrun);
         std::vector<int> want3(ns, 0), want5(ns, 0), want7(ns, 0), yo5(ns, 0), yo7(ns, 0);
         for (int si = 0; si < ns; ++si) {
@@ -980,7 +1071,8 @@ mcb_ctx *mcb_create(const mcb_params *params, int N, const double *SL, int batch
         return nullptr;
     };
     if (!params || !SL || N < 2 || N > MCB_NMAX || batch_max < 1 || batch_max > 4096) return fail(MCB_ERR_ARG);
-    if ((flags & 0xff) != MCB_PROJ_FP64) return fail(MCB_ERR_ARG);
+    const int proj = flags & 0xff;
+    if (proj != MCB_PROJ_FP64 && proj != MCB_PROJ_NS_BF16 && proj != MCB_PROJ_NS_TF32) return fail(MCB_ERR_ARG);
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(MCB_ERR_NODEV);
     mcb_ctx *c = new mcb_ctx();
@@ -1015,6 +1107,14 @@ mcb_ctx *mcb_create(const mcb_params *params, int N, const double *SL, int batch
     if (rc == MCB_OK) chk(cudaMalloc(&c->d_toutv, (size_t)batch_max * c->tcap_out * sizeof(double)));
     if (rc == MCB_OK) chk(cudaMalloc(&c->d_tbnd, (size_t)batch_max * c->tcap_bnd * sizeof(unsigned int)));
     if (rc == MCB_OK) chk(cudaMalloc(&c->d_tbndv, (size_t)batch_max * c->tcap_bnd * sizeof(double)));
+    c->proj = proj;
+    if (rc == MCB_OK && proj != MCB_PROJ_FP64) {
+        rc = c->ns.init(proj, N, batch_max, c->st);
+        if (rc != MCB_OK) c->err = "Newton-Schulz buffers or cuBLAS handle";
+        if (rc == MCB_OK) chk(cudaMalloc(&c->d_hlist, batch_max * sizeof(int)));
+        if (rc == MCB_OK) chk(cudaMalloc(&c->d_hkeys, batch_max * sizeof(unsigned long long)));
+        if (rc == MCB_OK) chk(cudaMalloc(&c->d_hsign, (size_t)batch_max * N * N));
+    }
     if (rc != MCB_OK) {
         if (status) *status = rc;
         mcb_destroy(c);
@@ -1028,8 +1128,10 @@ void mcb_destroy(mcb_ctx *c) {
     if (!c) return;
     if (c->st) cudaStreamSynchronize(c->st);
     for (auto &m : c->mem) free_slot(m);
+    c->ns.destroy();
     void *ps[] = {c->d_SL, c->d_slots, c->d_partials, c->d_lists, c->d_fixed, c->d_trisel, c->d_tout, c->d_toutv,
-                  c->d_tbnd, c->d_tbndv, c->d_sajobs, c->d_perm, c->d_saout, c->d_saval};
+                  c->d_tbnd, c->d_tbndv, c->d_sajobs, c->d_perm, c->d_saout, c->d_saval,
+                  c->d_hlist, c->d_hkeys, c->d_hsign};
     for (void *p : ps)
         if (p) cudaFree(p);
     for (auto &p : c->pending) { cudaEventDestroy(p.second.first); cudaEventDestroy(p.second.second); }
@@ -1048,6 +1150,22 @@ double mcb_get_lb(const mcb_ctx *c, int *sol) {
 }
 void mcb_set_diff(mcb_ctx *c, double d) { c->diff = d; }
 double mcb_get_diff(const mcb_ctx *c) { return c->diff; }
+int mcb_ns_options(mcb_ctx *c, int operands, double l0) {
+    if (!c || c->proj == MCB_PROJ_FP64) return MCB_ERR_ARG;
+    return c->ns.configure(operands, l0);
+}
+int mcb_ns_schedule(const mcb_ctx *c, int cap, float *a, float *b, int *accurate) {
+    if (!c || c->proj == MCB_PROJ_FP64) return 0;
+    int k = 0;
+    for (const NsStep &s : c->ns.steps) {
+        if (k >= cap) break;
+        if (a) a[k] = s.a;
+        if (b) b[k] = s.b;
+        if (accurate) accurate[k] = s.accurate;
+        ++k;
+    }
+    return (int)c->ns.steps.size();
+}
 void mcb_set_trials(mcb_ctx *c, int p, int h) { c->prm.Pent_Trials = p; c->prm.Hepta_Trials = h; }
 void mcb_get_trials(const mcb_ctx *c, int *p, int *h) { *p = c->prm.Pent_Trials; *h = c->prm.Hepta_Trials; }
 

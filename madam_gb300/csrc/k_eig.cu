@@ -7,6 +7,7 @@
 // back-transforms (dormtr).  These kernels do the same four steps on the GPU,
 // one CTA per node, FP64 throughout, with full-precision bisection.
 #include "mcb_dev.cuh"
+#include "ns.h"
 #include "kernels.h"
 
 namespace mcb {
@@ -370,11 +371,15 @@ __global__ void k_canon_scale(Slot *slots, int gate) {
 //   mode 1 (ADMM step, admm.c:574-585 and the residual terms of :600-665):
 //           X <- sigma X+ (full), Q <- X+ - W (full), partial sums per tile
 //           of ||X+ - X_old/sigma||^2, <L, X>, ||diag X - 1||^2 into s.dwork2
+//   modes 2 / 3: as 1 / 0, with X+ = (W + (G + G^T) / 2) / 2 from G = W sign(W)
+//           (the Newton-Schulz form; G padded with leading dimension gld)
 constexpr int TS = 32;
-__global__ void __launch_bounds__(256) k_syrk_post(Slot *slots, int mode, double *partials, int ptile) {
+__global__ void __launch_bounds__(256) k_syrk_post(Slot *slots, int mode, double *partials, int ptile,
+                                                   const double *G, int gld, size_t gstride) {
     Slot &s = slots[blockIdx.y];
-    if (!gated(s, mode)) return;
-    const int n = s.n, M = s.M;
+    const int admm = mode == 1 || mode == 2;
+    if (!gated(s, admm)) return;
+    const int n = s.n, M = mode >= 2 ? 0 : s.M;
     const int nt = (n + TS - 1) / TS;
     const int tile = blockIdx.x;
     if (tile >= nt * (nt + 1) / 2) return;
@@ -408,10 +413,14 @@ __global__ void __launch_bounds__(256) k_syrk_post(Slot *slots, int mode, double
     for (int r = 0; r < 4; ++r) {
         int i = i0 + ty * 4 + r, j = j0 + tx;
         if (i >= n || j >= n || i < j) continue;
-        double xp = acc[r];
         size_t ij = i + (size_t)j * n, ji = j + (size_t)i * n;
         double w = s.W[ij];
-        if (mode == 0) {
+        double xp = acc[r];
+        if (mode >= 2) {
+            const double *Gb = G + (size_t)blockIdx.y * gstride;
+            xp = 0.5 * (w + 0.5 * (Gb[i + (size_t)j * gld] + Gb[j + (size_t)i * gld]));
+        }
+        if (!admm) {
             s.X[ij] = xp;
             s.X[ji] = xp;
             s.Q[ij] = xp - w;
@@ -430,7 +439,7 @@ __global__ void __launch_bounds__(256) k_syrk_post(Slot *slots, int mode, double
             if (i == j) p_diag += (xn - 1.0) * (xn - 1.0);
         }
     }
-    if (mode == 1) {
+    if (admm) {
         double a = block_sum(p_dres, red);
         double b = block_sum(p_primal, red);
         double c = block_sum(p_diag, red);
@@ -500,8 +509,18 @@ int syrk_tiles(int nmax) {
 void launch_syrk_post(Slot *d_slots, int nslots, int nmax, int mode, double *partials, cudaStream_t st) {
     int T = syrk_tiles(nmax);
     dim3 g(T, nslots);
-    k_syrk_post<<<g, 256, 0, st>>>(d_slots, mode, partials, T);
+    k_syrk_post<<<g, 256, 0, st>>>(d_slots, mode, partials, T, nullptr, 0, 0);
     if (mode == 1) k_syrk_reduce<<<nslots, 256, 0, st>>>(d_slots, partials, T);
+}
+void launch_ns_post(Slot *d_slots, int nslots, int nmax, double *partials, const double *G, int npad, size_t stride,
+                    cudaStream_t st) {
+    int T = syrk_tiles(nmax);
+    k_syrk_post<<<dim3(T, nslots), 256, 0, st>>>(d_slots, 2, partials, T, G, npad, stride);
+    k_syrk_reduce<<<nslots, 256, 0, st>>>(d_slots, partials, T);
+}
+void launch_ns_post0(Slot *d_slots, int nslots, int nmax, const double *G, int npad, size_t stride, cudaStream_t st) {
+    int T = syrk_tiles(nmax);
+    k_syrk_post<<<dim3(T, nslots), 256, 0, st>>>(d_slots, 3, nullptr, T, G, npad, stride);
 }
 
 size_t eig_dwork_doubles(int nmax) { return (size_t)8 * 6 * nmax; }

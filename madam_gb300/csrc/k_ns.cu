@@ -1,0 +1,358 @@
+// k_ns.cu -- kernels and host orchestration of the Newton-Schulz PSD projection
+// (the chosen form, see ns.h) and of the GPU hyperplane rounding used by its
+// heuristic.
+#include <cublas_v2.h>
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <vector>
+
+#include "../../include/mcbound.h"
+#include "mcb_dev.cuh"
+#include "ns.h"
+
+namespace mcb {
+
+namespace {
+constexpr int TT = 32;  // tile edge of the copy kernels
+
+// ||W||_F from the lower triangle (an upper bound on the spectral radius)
+__global__ void __launch_bounds__(512) k_ns_alpha(Slot *slots, int gate) {
+    Slot &s = slots[blockIdx.x];
+    if (!gated(s, gate)) return;
+    const int n = s.n;
+    __shared__ double red[40];
+    double a = 0.0;
+    for (int j = threadIdx.x >> 5; j < n; j += blockDim.x >> 5) {
+        const double *col = s.W + (size_t)j * n;
+        for (int i = j + (threadIdx.x & 31); i < n; i += 32) {
+            double w = col[i];
+            a += (i == j ? 1.0 : 2.0) * w * w;
+        }
+    }
+    a = block_sum(a, red);
+    if (threadIdx.x == 0) s.acc[ACC_NS_ALPHA] = sqrt(a);
+}
+
+// Wd = W (full, FP64, padded to npad with zeros), S = W / alpha (FP32).
+// W holds the lower triangle; upper tiles are read through their mirror and
+// transposed in shared memory so that both reads and writes are coalesced.
+__global__ void __launch_bounds__(256) k_ns_scale(Slot *slots, int npad, size_t stride, float *S, double *Wd,
+                                                  int gate) {
+    Slot &s = slots[blockIdx.y];
+    if (!gated(s, gate)) return;
+    const int n = s.n, nt = (npad + TT - 1) / TT;
+    const int ti = blockIdx.x % nt, tj = blockIdx.x / nt;
+    if (tj >= nt) return;
+    const int I = ti >= tj ? ti : tj, J = ti >= tj ? tj : ti;
+    __shared__ double sh[TT][TT + 1];
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    for (int c = ty; c < TT; c += 8) {
+        int r = I * TT + tx, q = J * TT + c;
+        sh[c][tx] = (r < n && q < n) ? s.W[r + (size_t)q * n] : 0.0;
+    }
+    __syncthreads();
+    const double alpha = s.acc[ACC_NS_ALPHA];
+    const double inv = alpha > 0.0 ? 1.0 / alpha : 0.0;
+    float *Sb = S + (size_t)blockIdx.y * stride;
+    double *Wb = Wd + (size_t)blockIdx.y * stride;
+    for (int c = ty; c < TT; c += 8) {
+        int i = ti * TT + tx, j = tj * TT + c;
+        if (i >= npad || j >= npad) continue;
+        double v;
+        if (ti > tj) v = sh[c][tx];
+        else if (ti < tj) v = sh[tx][c];
+        else v = tx >= c ? sh[c][tx] : sh[tx][c];
+        if (i >= n || j >= n) v = 0.0;
+        size_t o = i + (size_t)j * npad;
+        Wb[o] = v;
+        Sb[o] = (float)(v * inv);
+    }
+}
+
+__global__ void k_ns_diag(Slot *slots, int npad, size_t stride, float *T, float a, int gate) {
+    Slot &s = slots[blockIdx.x];
+    if (!gated(s, gate)) return;
+    float *Tb = T + (size_t)blockIdx.x * stride;
+    for (int i = threadIdx.x; i < s.n; i += blockDim.x) Tb[i + (size_t)i * npad] += a;
+}
+
+// Sd = S in FP64; M = number of positive eigenvalues = (n + trace S) / 2 rounded
+__global__ void __launch_bounds__(256) k_ns_finish(Slot *slots, int npad, size_t stride, const float *S, double *Sd,
+                                                   int gate) {
+    Slot &s = slots[blockIdx.y];
+    if (!gated(s, gate)) return;
+    const float *Sb = S + (size_t)blockIdx.y * stride;
+    double *Db = Sd + (size_t)blockIdx.y * stride;
+    const size_t tot = (size_t)npad * npad;
+    for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < tot; q += (size_t)gridDim.x * blockDim.x)
+        Db[q] = (double)Sb[q];
+    if (blockIdx.x == 0) {
+        __shared__ double red[40];
+        double t = 0.0;
+        for (int i = threadIdx.x; i < s.n; i += blockDim.x) t += (double)Sb[i + (size_t)i * npad];
+        t = block_sum(t, red);
+        if (threadIdx.x == 0) {
+            s.acc[ACC_NS_TRACE] = t;
+            int M = (int)llrint(0.5 * ((double)s.n + t));
+            s.M = M < 0 ? 0 : (M > s.n ? s.n : M);
+        }
+    }
+}
+
+// --- heuristic: hyperplane signs of X v -------------------------------------
+__global__ void __launch_bounds__(256) k_heur_xf(Slot *slots, const int *list, int npad, size_t stride, float *Xf) {
+    const int si = list[blockIdx.y];
+    Slot &s = slots[si];
+    const int n = s.n;
+    float *Xb = Xf + (size_t)si * stride;
+    const size_t tot = (size_t)npad * npad;
+    for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < tot; q += (size_t)gridDim.x * blockDim.x) {
+        int j = (int)(q / npad), i = (int)(q - (size_t)j * npad);
+        Xb[q] = (i < n && j < n) ? (float)s.X[i + (size_t)j * n] : 0.0f;
+    }
+}
+
+// V[:, c] = the n draws (uniform in [-0.5, 0.5)) of stream key2(key, c): draw i of a
+// counter stream is mix64(key + (i + 1) * golden), see Stream::next
+__global__ void __launch_bounds__(256) k_heur_vec(Slot *slots, const int *list, const unsigned long long *keys,
+                                                  int count, int npad, size_t stride, float *V) {
+    const int si = list[blockIdx.y];
+    const int n = slots[si].n;
+    const uint64_t key = keys[blockIdx.y];
+    float *Vb = V + (size_t)si * stride;
+    const size_t tot = (size_t)npad * count;
+    for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < tot; q += (size_t)gridDim.x * blockDim.x) {
+        int c = (int)(q / npad), i = (int)(q - (size_t)c * npad);
+        float v = 0.0f;
+        if (i < n) {
+            uint64_t kc = key2(key, (uint64_t)c);
+            uint64_t z = mix64(kc + (uint64_t)(i + 1) * 0x9E3779B97F4A7C15ull);
+            v = (float)((double)(z >> 11) * 0x1.0p-53 - 0.5);
+        }
+        Vb[q] = v;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_heur_sign(Slot *slots, const int *list, int count, int npad, size_t stride,
+                                                   const float *H, unsigned char *out, size_t out_stride) {
+    const int si = list[blockIdx.y];
+    const int n = slots[si].n;
+    const float *Hb = H + (size_t)si * stride;
+    unsigned char *ob = out + (size_t)blockIdx.y * out_stride;
+    const size_t tot = (size_t)n * count;
+    for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < tot; q += (size_t)gridDim.x * blockDim.x) {
+        int c = (int)(q / n), i = (int)(q - (size_t)c * n);
+        ob[q] = Hb[i + (size_t)c * npad] < 0.0f ? 1 : 0;
+    }
+}
+
+inline int cdiv(size_t a, int b) { return (int)((a + b - 1) / b); }
+inline int grid_for(size_t tot) {
+    int g = cdiv(tot, 256);
+    return g < 1 ? 1 : (g > 1184 ? 1184 : g);
+}
+
+}  // namespace
+
+void launch_ns_prep(Slot *d, int ns, int npad, size_t stride, float *S, double *Wd, int gate, cudaStream_t st) {
+    k_ns_alpha<<<ns, 512, 0, st>>>(d, gate);
+    int nt = (npad + TT - 1) / TT;
+    k_ns_scale<<<dim3(nt * nt, ns), 256, 0, st>>>(d, npad, stride, S, Wd, gate);
+}
+void launch_ns_diag(Slot *d, int ns, int npad, size_t stride, float *T, float a, int gate, cudaStream_t st) {
+    (void)npad;
+    k_ns_diag<<<ns, 256, 0, st>>>(d, npad, stride, T, a, gate);
+}
+void launch_ns_finish(Slot *d, int ns, int npad, size_t stride, const float *S, double *Sd, int gate,
+                      cudaStream_t st) {
+    int g = grid_for((size_t)npad * npad);
+    g = g > 64 ? 64 : g;
+    k_ns_finish<<<dim3(g, ns), 256, 0, st>>>(d, npad, stride, S, Sd, gate);
+}
+void launch_heur_xf(Slot *d, const int *slots, int nslots, int npad, size_t stride, float *Xf, cudaStream_t st) {
+    int g = grid_for((size_t)npad * npad);
+    g = g > 64 ? 64 : g;
+    k_heur_xf<<<dim3(g, nslots), 256, 0, st>>>(d, slots, npad, stride, Xf);
+}
+void launch_heur_vectors(Slot *d, const int *slots, const unsigned long long *keys, int nslots, int count, int npad,
+                         size_t stride, float *V, cudaStream_t st) {
+    int g = grid_for((size_t)npad * count);
+    g = g > 64 ? 64 : g;
+    k_heur_vec<<<dim3(g, nslots), 256, 0, st>>>(d, slots, keys, count, npad, stride, V);
+}
+void launch_heur_signs(Slot *d, const int *slots, int nslots, int count, int npad, size_t stride, const float *H,
+                       unsigned char *out, size_t out_stride, cudaStream_t st) {
+    int g = grid_for((size_t)npad * count);
+    g = g > 64 ? 64 : g;
+    k_heur_sign<<<dim3(g, nslots), 256, 0, st>>>(d, slots, count, npad, stride, H, out, out_stride);
+}
+
+// --- schedule and host orchestration ---------------------------------------
+std::vector<NsStep> ns_schedule(double l0, double safety, double eps) {
+    std::vector<NsStep> st;
+    double l = l0;
+    auto p = [](double y) { return 1.5 * y - 0.5 * y * y * y; };
+    while (1.0 - l > eps && st.size() < 64) {
+        double k2 = 3.0 * (1.0 - safety) / (1.0 + l + l * l);
+        double k = k2 > 1.0 ? sqrt(k2) : 1.0;
+        NsStep s;
+        s.a = (float)(1.5 * k);
+        s.b = (float)(-0.5 * k * k * k);
+        s.accurate = l > 0.9;
+        double nl = p(k * l) < p(k) ? p(k * l) : p(k);
+        st.push_back(s);
+        l = nl;
+    }
+    // at least two accurate steps: they remove the low-precision rounding
+    int acc = 0;
+    for (auto &s : st) acc += s.accurate;
+    while (acc < 2) {
+        st.push_back({1.5f, -0.5f, 1});
+        ++acc;
+    }
+    return st;
+}
+
+int NsProj::init(int form_, int nmax_, int cap_, cudaStream_t st) {
+    form = form_;
+    nmax = nmax_;
+    cap = cap_;
+    int np = (nmax + 15) / 16 * 16;
+    stride = (size_t)np * np;
+    if (cublasCreate(&h) != CUBLAS_STATUS_SUCCESS) return MCB_ERR_CUDA;
+    cublasSetStream(h, st);
+    const size_t tot = stride * (size_t)cap;
+    if (cudaMalloc(&S, tot * sizeof(float)) != cudaSuccess) return MCB_ERR_NOMEM;
+    if (cudaMalloc(&S2, tot * sizeof(float)) != cudaSuccess) return MCB_ERR_NOMEM;
+    if (cudaMalloc(&T, tot * sizeof(float)) != cudaSuccess) return MCB_ERR_NOMEM;
+    if (cudaMalloc(&Wd, tot * sizeof(double)) != cudaSuccess) return MCB_ERR_NOMEM;
+    if (cudaMalloc(&Sd, tot * sizeof(double)) != cudaSuccess) return MCB_ERR_NOMEM;
+    if (cudaMalloc(&Gd, tot * sizeof(double)) != cudaSuccess) return MCB_ERR_NOMEM;
+    if (cudaMalloc(&dptr, 6 * (size_t)cap * sizeof(void *)) != cudaSuccess) return MCB_ERR_NOMEM;
+    hptr.assign(6 * (size_t)cap, nullptr);
+    steps = ns_schedule(l0, 0.02, 1e-7);
+    return MCB_OK;
+}
+
+int NsProj::configure(int operands_, double l0_) {
+    if (operands_ < MCB_NS_OPERANDS_NATIVE || operands_ > MCB_NS_OPERANDS_FP32 || !(l0_ > 0.0 && l0_ < 0.5))
+        return MCB_ERR_ARG;
+    operands = operands_;
+    l0 = l0_;
+    steps = ns_schedule(l0, 0.02, 1e-7);
+    return MCB_OK;
+}
+
+void NsProj::destroy() {
+    void *ps[] = {S, S2, T, Wd, Sd, Gd, dptr};
+    for (void *p : ps)
+        if (p) cudaFree(p);
+    S = S2 = T = nullptr;
+    Wd = Sd = Gd = nullptr;
+    dptr = nullptr;
+    if (h) cublasDestroy(h);
+    h = nullptr;
+}
+
+int NsProj::set_live(const std::vector<int> &slots, int npad_, cudaStream_t st) {
+    live = (int)slots.size();
+    npad = npad_;
+    for (int k = 0; k < live; ++k) {
+        size_t o = slot_offset(slots[k]);
+        hptr[0 * cap + k] = S + o;
+        hptr[1 * cap + k] = S2 + o;
+        hptr[2 * cap + k] = T + o;
+        hptr[3 * cap + k] = Wd + o;
+        hptr[4 * cap + k] = Sd + o;
+        hptr[5 * cap + k] = Gd + o;
+    }
+    if (cudaMemcpyAsync(dptr, hptr.data(), 6 * (size_t)cap * sizeof(void *), cudaMemcpyHostToDevice, st) !=
+        cudaSuccess)
+        return MCB_ERR_CUDA;
+    // the staging vector is rewritten by the next call only: wait for the copy
+    if (cudaStreamSynchronize(st) != cudaSuccess) return MCB_ERR_CUDA;
+    return MCB_OK;
+}
+
+namespace {
+cublasStatus_t gemm32(cublasHandle_t h, int np, float alpha, void **A, void **B, float beta, void **C, int batch,
+                      cublasComputeType_t ct) {
+    return cublasGemmBatchedEx(h, CUBLAS_OP_N, CUBLAS_OP_N, np, np, np, &alpha, (const void *const *)A, CUDA_R_32F,
+                               np, (const void *const *)B, CUDA_R_32F, np, &beta, (void *const *)C, CUDA_R_32F, np,
+                               batch, ct, CUBLAS_GEMM_DEFAULT);
+}
+}  // namespace
+
+int NsProj::sign(Slot *d_slots, int ns, int gate, cudaStream_t st) {
+    if (live == 0) return MCB_OK;
+    cublasSetStream(h, st);
+    void **pS = dptr, **pS2 = dptr + cap, **pT = dptr + 2 * cap;
+    // growth steps: one pass of the form's type (NATIVE), its FP32-accurate split
+    // (SPLIT: three BF16 pieces per operand, nine products), or FP32 FMA (FP32);
+    // the closing steps always FP32-accurate
+    const cublasComputeType_t split = CUBLAS_COMPUTE_32F_EMULATED_16BFX9;
+    cublasComputeType_t lo = form == MCB_PROJ_NS_TF32 ? CUBLAS_COMPUTE_32F_FAST_TF32 : CUBLAS_COMPUTE_32F_FAST_16BF;
+    if (operands == MCB_NS_OPERANDS_SPLIT) lo = split;
+    if (operands == MCB_NS_OPERANDS_FP32) lo = CUBLAS_COMPUTE_32F;
+    const cublasComputeType_t hi = operands == MCB_NS_OPERANDS_FP32 ? CUBLAS_COMPUTE_32F : split;
+    float *cur = S, *nxt = S2;
+    void **pc = pS, **pn = pS2;
+    const double g = 2.0 * (double)npad * npad * npad * live;
+    for (const NsStep &stp : steps) {
+        cublasComputeType_t ct = stp.accurate ? hi : lo;
+        // T = b S^2 + a I, then S' = S T
+        if (gemm32(h, npad, stp.b, pc, pc, 0.0f, pT, live, ct) != CUBLAS_STATUS_SUCCESS) return MCB_ERR_CUDA;
+        launch_ns_diag(d_slots, ns, npad, stride, T, stp.a, gate, st);
+        if (gemm32(h, npad, 1.0f, pc, pT, 0.0f, pn, live, ct) != CUBLAS_STATUS_SUCCESS) return MCB_ERR_CUDA;
+        (stp.accurate ? flops_hi : flops_lo) += 2.0 * g;
+        float *t = cur; cur = nxt; nxt = t;
+        void **tp = pc; pc = pn; pn = tp;
+    }
+    launch_ns_finish(d_slots, ns, npad, stride, cur, Sd, gate, st);
+    return MCB_OK;
+}
+
+int NsProj::product(cudaStream_t st) {
+    if (live == 0) return MCB_OK;
+    cublasSetStream(h, st);
+    void **pW = dptr + 3 * cap, **pSd = dptr + 4 * cap, **pG = dptr + 5 * cap;
+    const double one = 1.0, zero = 0.0;
+    if (cublasGemmBatchedEx(h, CUBLAS_OP_N, CUBLAS_OP_N, npad, npad, npad, &one, (const void *const *)pW, CUDA_R_64F,
+                            npad, (const void *const *)pSd, CUDA_R_64F, npad, &zero, (void *const *)pG, CUDA_R_64F,
+                            npad, live, CUBLAS_COMPUTE_64F, CUBLAS_GEMM_DEFAULT) != CUBLAS_STATUS_SUCCESS)
+        return MCB_ERR_CUDA;
+    flops_fp64 += 2.0 * (double)npad * npad * npad * live;
+    return MCB_OK;
+}
+
+int NsProj::hyperplanes(Slot *d_slots, const std::vector<int> &slots, const int *d_list,
+                        const unsigned long long *d_keys, int count, int npad_, unsigned char *d_out, size_t out_stride,
+                        cudaStream_t st) {
+    const int k = (int)slots.size();
+    if (k == 0) return MCB_OK;
+    for (int q = 0; q < k; ++q) {
+        size_t o = slot_offset(slots[q]);
+        hptr[0 * cap + q] = S + o;   // X in FP32
+        hptr[1 * cap + q] = T + o;   // hyperplane normals
+        hptr[2 * cap + q] = S2 + o;  // X V
+    }
+    if (cudaMemcpyAsync(dptr, hptr.data(), 3 * (size_t)cap * sizeof(void *), cudaMemcpyHostToDevice, st) != cudaSuccess)
+        return MCB_ERR_CUDA;
+    if (cudaStreamSynchronize(st) != cudaSuccess) return MCB_ERR_CUDA;
+    live = 0;  // the live-slot arrays were overwritten
+    launch_heur_xf(d_slots, d_list, k, npad_, stride, S, st);
+    launch_heur_vectors(d_slots, d_list, d_keys, k, count, npad_, stride, T, st);
+    cublasSetStream(h, st);
+    const float one = 1.0f, zero = 0.0f;
+    if (cublasGemmBatchedEx(h, CUBLAS_OP_N, CUBLAS_OP_N, npad_, count, npad_, &one, (const void *const *)dptr,
+                            CUDA_R_32F, npad_, (const void *const *)(dptr + cap), CUDA_R_32F, npad_, &zero,
+                            (void *const *)(dptr + 2 * cap), CUDA_R_32F, npad_, k, CUBLAS_COMPUTE_32F_FAST_TF32,
+                            CUBLAS_GEMM_DEFAULT) != CUBLAS_STATUS_SUCCESS)
+        return MCB_ERR_CUDA;
+    launch_heur_signs(d_slots, d_list, k, count, npad_, stride, S2, d_out, out_stride, st);
+    return MCB_OK;
+}
+
+}  // namespace mcb

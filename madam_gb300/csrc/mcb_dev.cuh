@@ -62,6 +62,8 @@ enum Acc {
     ACC_SIGMA_LAST,   // sigma of the last ADMM iteration (scales the heuristic's factor)
     // IPM state (ipm_mc_pk.c)
     ACC_MU, ACC_PHI, ACC_PSI, ACC_AP, ACC_AD, ACC_IPM_IT, ACC_IPM_DONE, ACC_IPM_INFO,
+    // Newton-Schulz projection: scale of W and trace of sign(W)
+    ACC_NS_ALPHA, ACC_NS_TRACE,
     kAcc = 32
 };
 

@@ -9,6 +9,7 @@
 #include "host_cuts.h"
 #include "kernels.h"
 #include "mcb_dev.cuh"
+#include "ns.h"
 
 using namespace mcb;
 
@@ -112,6 +113,24 @@ int upload_one(OneSlot &S, const HostCuts &H) {
     return cuda_rc(S.push());
 }
 
+// Newton-Schulz form of the projection on one matrix (Xp full, Q lower, M)
+int project_ns(OneSlot &S, int n, int proj) {
+    NsProj P;
+    int rc = P.init(proj & 0xf, n, 1, 0);
+    if (rc == MCB_OK && (proj >> 4)) rc = P.configure(((proj >> 4) & 0xf) - 1, P.l0);
+    if (rc == MCB_OK) {
+        const int npad = (n + 15) / 16 * 16;
+        rc = P.set_live({0}, npad, 0);
+        if (rc == MCB_OK) launch_ns_prep(S.d, 1, npad, P.stride, P.S, P.Wd, 0, 0);
+        if (rc == MCB_OK) rc = P.sign(S.d, 1, 0, 0);
+        if (rc == MCB_OK) rc = P.product(0);
+        if (rc == MCB_OK) launch_ns_post0(S.d, 1, n, P.Gd, npad, P.stride, 0);
+        if (rc == MCB_OK && cudaDeviceSynchronize() != cudaSuccess) rc = MCB_ERR_CUDA;
+    }
+    P.destroy();
+    return rc;
+}
+
 }  // namespace
 
 extern "C" {
@@ -158,11 +177,23 @@ int mcb_op_Bt(int n, double *X, int ntri, const int *tri, int npent, const int *
 
 int mcb_project_psd(int n, const double *W, int proj, double *Xp, double *Q, double *Z, double *evals, int *M) {
     if (n < 1 || n > MCB_NMAX || !W || !M) return MCB_ERR_ARG;
-    if (proj != MCB_PROJ_FP64) return MCB_ERR_ARG;
+    const int form = proj & 0xf;
+    if (proj & ~0xff) return MCB_ERR_ARG;
+    if (form != MCB_PROJ_FP64 && form != MCB_PROJ_NS_BF16 && form != MCB_PROJ_NS_TF32) return MCB_ERR_ARG;
+    if (form == MCB_PROJ_FP64 && proj != form) return MCB_ERR_ARG;
     if (int rc = check_dev()) return rc;
     OneSlot S(n);
     if (S.push()) return MCB_ERR_CUDA;
     cudaMemcpy(S.h.W, W, (size_t)n * n * sizeof(double), cudaMemcpyHostToDevice);
+    if (form != MCB_PROJ_FP64) {
+        // no eigenvectors in this form: Z and evals are left untouched
+        if (int rc = project_ns(S, n, proj)) return rc;
+        if (S.pull()) return MCB_ERR_CUDA;
+        *M = S.h.M;
+        if (Xp) cudaMemcpy(Xp, S.h.X, (size_t)n * n * sizeof(double), cudaMemcpyDeviceToHost);
+        if (Q) cudaMemcpy(Q, S.h.Q, (size_t)n * n * sizeof(double), cudaMemcpyDeviceToHost);
+        return cuda_rc(cudaDeviceSynchronize());
+    }
     launch_sym_copy(S.d, 1, n, 0, 0, 0);
     launch_tridiag(S.d, 1, n, 0, 0);
     launch_bisect(S.d, 1, n, 1e-8, 0, 0, 0);

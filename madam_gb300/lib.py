@@ -17,6 +17,12 @@ NMAX = 1024
 
 OK, ERR_ARG, ERR_CUDA, ERR_NOMEM, ERR_NUMERIC, ERR_CAPACITY, ERR_ITER, ERR_NODEV = 0, -1, -2, -3, -4, -5, -6, -7
 PROJ_FP64, PROJ_NS_BF16, PROJ_NS_TF32 = 0x0, 0x1, 0x2
+NS_OPERANDS_NATIVE, NS_OPERANDS_SPLIT, NS_OPERANDS_FP32 = 0, 1, 2
+
+
+def PROJ_OPERANDS(op):
+    """Operand choice of the Newton-Schulz forms for `project` (MCB_PROJ_OPERANDS)."""
+    return (op + 1) << 4
 FLAG_PROFILE, FLAG_LEARNED = 0x100, 0x200
 
 PARAM_FIELDS = [
@@ -121,6 +127,8 @@ def lib():
     L.mcb_kernel_work.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
     L.mcb_transfer_stats.argtypes = [C.c_void_p, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]
     L.mcb_measure_fp64_peak.restype = C.c_double
+    L.mcb_ns_options.argtypes = [C.c_void_p, C.c_int, C.c_double]
+    L.mcb_ns_schedule.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
     L.mcb_launch_count.restype = C.c_longlong
     L.mcb_launch_count.argtypes = [C.c_void_p]
     _lib = L
@@ -230,6 +238,15 @@ class Context:
         a, b = C.c_longlong(), C.c_longlong()
         lib().mcb_transfer_stats(self.h, C.byref(a), C.byref(b))
         return a.value, b.value
+
+    def ns_options(self, operands=NS_OPERANDS_SPLIT, l0=1e-6):
+        _check(lib().mcb_ns_options(self.h, operands, l0), self.h)
+
+    def ns_schedule(self):
+        cap = 64
+        a, b, acc = (C.c_float * cap)(), (C.c_float * cap)(), (C.c_int * cap)()
+        k = lib().mcb_ns_schedule(self.h, cap, C.cast(a, C.c_void_p), C.cast(b, C.c_void_p), C.cast(acc, C.c_void_p))
+        return [(a[i], b[i], acc[i]) for i in range(min(k, cap))]
 
     def reset_kernel_stats(self):
         lib().mcb_reset_kernel_stats(self.h)

@@ -1,0 +1,142 @@
+"""The chosen form: Newton-Schulz PSD projection on the tensor cores.
+
+Checks (1) the projection against an FP64 eigendecomposition (numpy.linalg.eigh)
+for FP32-accurate operands (default) and for one-pass operands, whose rounding
+floor is stated; (2) node bounds against the CPU oracle's FP64 method: the
+bound is the same safe dual bound n lambda_max(L - Diag y - B^T s) + sum y +
+sum s, so it stays valid whatever the projection's error, and it agrees with the
+FP64 method to the ADMM's own stopping tolerance (minTol = 1e-3); (3) whole
+branch-and-bound runs reach the reference's optimum and optimal cut.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from madam_gb300 import graphs as G
+
+pytestmark = pytest.mark.gpu
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+FIXTURES = json.load(open(os.path.join(HERE, "golden", "reference_bab.json")))["instances"]
+
+
+def _proj_eigh(W):
+    w, V = np.linalg.eigh(W)
+    k = w > 1e-8
+    return (V[:, k] * w[k]) @ V[:, k].T, int(k.sum())
+
+
+def _spectra(n, rng):
+    A = rng.standard_normal((n, n))
+    gauss = (A + A.T) / np.sqrt(2 * n)
+    U, _ = np.linalg.qr(rng.standard_normal((n, n)))
+    r = max(2, n // 20)
+    # ADMM-like: a few clearly positive eigenvalues (X / sigma), the rest negative (-Q)
+    lam = np.concatenate([np.linspace(6.0, 0.3, r), -0.05 - 2.0 * np.abs(rng.standard_normal(n - r))])
+    return {"gauss": gauss, "admm": (U * lam) @ U.T}
+
+
+@pytest.mark.parametrize("n", [33, 130, 257, 512])
+@pytest.mark.parametrize("form", ["bf16", "tf32"])
+def test_ns_projection_against_eigh(gpu_lib, n, form):
+    M = gpu_lib
+    proj = M.PROJ_NS_BF16 if form == "bf16" else M.PROJ_NS_TF32
+    rng = np.random.default_rng(n)
+    for name, W in _spectra(n, rng).items():
+        Xr, Mr = _proj_eigh(W)
+        Xp, Q, Z, _ = M.project(W, proj)
+        err = np.linalg.norm(Xp - Xr) / np.linalg.norm(W)
+        # FP32-accurate operands: the error is the FP32 rounding of the iteration
+        assert err < 5e-6, (name, err)
+        assert np.array_equal(Xp, Xp.T)
+        assert np.allclose(np.tril(Q), np.tril(Xp - W), atol=1e-12)
+        if name == "admm":  # a spectral gap around 0: the count is exact
+            assert Z.shape[1] == Mr
+            assert np.isclose(np.trace(Xp), np.trace(Xr), rtol=1e-5)
+
+
+def test_ns_one_pass_operands_have_a_rounding_floor(gpu_lib):
+    """One pass of BF16/TF32 operands cannot resolve eigenvalues below their
+    rounding (~1e-3 of ||W||): the error floor that makes the default split."""
+    M = gpu_lib
+    rng = np.random.default_rng(5)
+    W = _spectra(256, rng)["gauss"]
+    Xr, _ = _proj_eigh(W)
+    Xn, _, _, _ = M.project(W, M.PROJ_NS_TF32 | M.PROJ_OPERANDS(M.NS_OPERANDS_NATIVE))
+    Xs, _, _, _ = M.project(W, M.PROJ_NS_TF32 | M.PROJ_OPERANDS(M.NS_OPERANDS_SPLIT))
+    en = np.linalg.norm(Xn - Xr) / np.linalg.norm(W)
+    es = np.linalg.norm(Xs - Xr) / np.linalg.norm(W)
+    assert 1e-5 < en < 5e-3
+    assert es < en / 100
+
+
+def test_ns_projection_zero_matrix(gpu_lib):
+    M = gpu_lib
+    Xp, Q, _, _ = M.project(np.zeros((20, 20)), M.PROJ_NS_BF16)
+    assert not Xp.any() and not Q.any()
+
+
+def test_ns_schedule_properties(gpu_lib):
+    """Scaled Newton-Schulz steps: p(x) = a x + b x^3 keeps [0, 1] in [0, 1], raises
+    the lower end of the spectrum interval from l0 to within 1e-7 of 1, and closes
+    with FP32-accurate steps."""
+    M = gpu_lib
+    n, e, w = G.gnp(20, 0.5, "pm1", seed=1)
+    ctx = M.Context(M.params(), G.extended_laplacian(n, e, w).ravel(order="F"), n, flags=M.PROJ_NS_BF16)
+    for l0 in (1e-3, 1e-6):
+        ctx.ns_options(M.NS_OPERANDS_SPLIT, l0)
+        st = ctx.ns_schedule()
+        lo, xs = l0, np.linspace(0, 1, 2001)
+        for a, b, acc in st:
+            assert np.all(a * xs + b * xs ** 3 <= 1 + 1e-6) and np.all(a * xs + b * xs ** 3 >= -1e-9)
+            lo = min(a * lo + b * lo ** 3, a + b)
+        assert lo > 1 - 1e-6
+        assert st[-1][2] == 1 and st[-2][2] == 1
+    with pytest.raises(M.MCBError):
+        ctx.ns_options(M.NS_OPERANDS_SPLIT, 0.7)
+    ctx.close()
+    with pytest.raises(M.MCBError):
+        M.Context(M.params(), G.extended_laplacian(n, e, w).ravel(order="F"), n).ns_options(0, 1e-6)
+
+
+@pytest.mark.parametrize("n,p,wts,seed,fixed,pent", [
+    (40, 0.5, "one", 2, {3: 1, 11: 0}, 1),
+    (64, 0.5, "pm1", 4, {}, 0),
+    (80, 0.1, "int10", 5, {7: 1}, 1),
+])
+def test_ns_node_bound_against_oracle(gpu_lib, orc, n, p, wts, seed, fixed, pent):
+    M = gpu_lib
+    nv, e, w = G.gnp(n, p, wts, seed=seed)
+    SL = G.extended_laplacian(nv, e, w).ravel(order="F")
+    oc = orc.Ctx(orc.shipped_params(include_Pent=pent, include_Hepta=0, use_diff=0), SL, nv,
+                 rng=orc.RNG_COUNTER, topk=orc.TOPK_CANONICAL, canon_sign=1)
+    bo, so = oc.evaluate(orc.make_node(nv - 1, fixed), rank=1)
+    for proj in (M.PROJ_NS_BF16, M.PROJ_NS_TF32):
+        ctx = M.Context(M.params(include_Pent=pent, include_Hepta=0, use_diff=0), SL, nv, flags=proj)
+        bg, sg = ctx.evaluate(M.node(fixed), rank=1)
+        assert abs(bg - bo) <= 2e-3 * abs(bo), (bg, bo)
+        # the node's best cut (found by either heuristic) never exceeds a safe bound
+        assert bg >= max(ctx.lb()[0], oc.lb()[0])
+        assert abs(sg.admm_iters - so.admm_iters) <= 0.25 * so.admm_iters + 20
+        ctx.close()
+
+
+@pytest.mark.parametrize("fx", FIXTURES, ids=lambda f: f["name"])
+def test_ns_branch_and_bound_reaches_reference_optimum(gpu_lib, fx):
+    M = gpu_lib
+    if fx["kind"] == "gnp":
+        n, e, w = G.gnp(*fx["args"][:3], seed=fx["args"][3])
+    else:
+        n, e, w = G.torus2d(fx["args"][0], fx["args"][1], seed=fx["args"][2])
+    SL = G.extended_laplacian(n, e, w).ravel(order="F")
+    ctx = M.Context(M.params(), SL, n, batch_max=4, flags=M.PROJ_NS_BF16)
+    r = ctx.bab(batch=4, max_nodes=2000)
+    assert r["opt"] == fx["opt"]
+    side = np.zeros(n, dtype=np.int32)
+    side[: n - 1] = r["sol"]
+    assert G.cut_value(n, e, w, side) == fx["opt"]
+    # every bound of the tree is a valid bound on the cut of its subtree; the root's on the optimum
+    assert r["root_bound"] >= fx["opt"]
+    ctx.close()
