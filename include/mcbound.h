@@ -52,7 +52,8 @@ enum mcb_status {
 #define MCB_NS_OPERANDS_NATIVE 0 /* one pass of the form's type (BF16 / TF32): rounding floor ~1e-3 */
 #define MCB_NS_OPERANDS_SPLIT 1  /* FP32-accurate: each operand split into three BF16 pieces (default) */
 #define MCB_NS_OPERANDS_FP32 2   /* FP32 FMA, no tensor cores (reference point) */
-#define MCB_FLAG_LEARNED 0x200 /* learned cut ranking + dual warm start (needs mcb_load_model) */
+#define MCB_FLAG_LEARNED 0x200 /* learned cut ranking + dual warm start (models set by mcb_set_models) */
+#define MCB_FLAG_LOG 0x400     /* log the learned models' training pairs (mcb_log_fetch) */
 
 /* Same fields, order and meaning as MADAM's Parameters (admm.h:57-89). */
 typedef struct mcb_params {
@@ -193,6 +194,42 @@ int mcb_separate_triangles(int n, const double *X, int K, double thr, int *out, 
  * getViolated_Pentagonal/HeptagonalInequalities call (cutting_planes.c:247-250,
  * 444-447).  ineq: k ints per run; values: the SA cost per run. */
 int mcb_qap_sa_batch(int n, const double *X, int k, int trials, uint64_t key, int *ineq, double *values);
+
+/* ---- learned cut ranking and dual warm start ----------------------------------
+ * No counterpart in the reference.  A small MLP (d inputs, two tanh layers of
+ * h1 and h2 units, one linear output; FP32), trained on the GPU by the library's
+ * own forward / backward / Adam kernels (mean squared error).  Host buffers in
+ * and out; X is row-major n x d.  Parameter vector layout:
+ * [W1 (h1 x d, row-major) | b1 | W2 (h2 x h1) | b2 | w3 (h2) | b3]. */
+typedef struct mcb_mlp mcb_mlp;
+mcb_mlp *mcb_mlp_create(int d_in, int h1, int h2, uint64_t seed, int *status);
+void mcb_mlp_destroy(mcb_mlp *mlp);
+int mcb_mlp_num_params(const mcb_mlp *mlp);
+int mcb_mlp_get_params(const mcb_mlp *mlp, float *params);
+int mcb_mlp_set_params(mcb_mlp *mlp, const float *params);  /* also resets Adam's moments */
+int mcb_mlp_predict(mcb_mlp *mlp, const float *X, int n, float *out);
+/* gradient of mean((f(X) - Y)^2) with respect to the parameters, and the loss */
+int mcb_mlp_gradient(mcb_mlp *mlp, const float *X, const float *Y, int n, float *grad, float *loss);
+/* `epochs` passes of Adam (beta 0.9 / 0.999) over shuffled minibatches; final_loss
+ * = the loss over all n samples after training */
+int mcb_mlp_train(mcb_mlp *mlp, const float *X, const float *Y, int n, int epochs, int batch, float lr,
+                  uint64_t seed, float *final_loss);
+
+/* Attach the models to a context (not owned; either may be null).  With
+ * MCB_FLAG_LEARNED the scorer ranks the 2K most violated triangles of each
+ * separation (cutting_planes.c:48-127 keeps the K most violated) and keeps the K
+ * best scores; mcb_bab hands each child its parent's final cuts (those through
+ * the branching variable dropped) with duals predicted by the warm model as the
+ * starting cut set.  Without a model that part is the plain method.  Both models
+ * take the 10 features documented in k_learn.cu and predict log(1 + dual). */
+int mcb_set_models(mcb_ctx *ctx, mcb_mlp *cut_scorer, mcb_mlp *warm_start);
+/* Training pairs logged under MCB_FLAG_LOG: which = 0 cut scorer (features at
+ * separation -> log(1 + dual after the next ADMM call)), 1 warm start (parent's
+ * final cut features with its dual -> log(1 + the child's final dual of the
+ * same cut, 0 if absent)); rows of 10 floats. */
+int mcb_log_count(const mcb_ctx *ctx, int which);
+int mcb_log_fetch(const mcb_ctx *ctx, int which, int cap, float *X, float *y);
+void mcb_log_clear(mcb_ctx *ctx);
 
 /* ---- instrumentation ---------------------------------------------------------
  * Per kernel class: launches and total device time (ms, CUDA events on the

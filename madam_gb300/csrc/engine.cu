@@ -14,6 +14,8 @@
 #include <cstdio>
 #include <cstring>
 #include <cstdlib>
+#include <map>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <thread>
@@ -25,6 +27,8 @@
 #include "kernels.h"
 #include "mcb_dev.cuh"
 #include "ns.h"
+#include "learn.h"
+#include "mlp.h"
 
 using namespace mcb;
 
@@ -33,12 +37,12 @@ namespace {
 const char *kClassNames[] = {"subproblem", "ipm",   "admm_rhs", "cg",        "admm_su", "build_W",
                              "sym_copy",   "tridiag", "bisect", "invit",     "backtrans", "canon_scale",
                              "syrk_post",  "admm_bx", "admm_finish", "safe_bound", "tri_sep", "sa",
-                             "ns_prep",    "ns_gemm", "ns_fp64", "heur_gpu"};
+                             "ns_prep",    "ns_gemm", "ns_fp64", "heur_gpu", "learned"};
 // unit of mcb_ctx::work per class: 1 = FP64 flops, 2 = bytes, 3 = tensor-core GEMM
 // flops (the Newton-Schulz steps, low-precision and FP32-accurate), 0 = not counted
-const int kWorkUnit[] = {0, 0, 2, 0, 0, 2, 2, 1, 0, 0, 1, 0, 1, 0, 0, 0, 0, 0, 2, 3, 1, 0};
+const int kWorkUnit[] = {0, 0, 2, 0, 0, 2, 2, 1, 0, 0, 1, 0, 1, 0, 0, 0, 0, 0, 2, 3, 1, 0, 0};
 enum KClass { K_SUB, K_IPM, K_RHS, K_CG, K_SU, K_W, K_SYMC, K_TRID, K_BIS, K_INV, K_BACK, K_CANON, K_SYRK,
-              K_BX, K_FIN, K_SAFE, K_TRI, K_SA, K_NSPREP, K_NSGEMM, K_NSREF, K_HEUR, K_NCLASS };
+              K_BX, K_FIN, K_SAFE, K_TRI, K_SA, K_NSPREP, K_NSGEMM, K_NSREF, K_HEUR, K_LEARN, K_NCLASS };
 
 struct DevBuf {
     void *p = nullptr;
@@ -61,6 +65,23 @@ struct SlotMem {
     double *e_coef = nullptr;
 };
 
+// A node's cuts at the end of its bound, in global vertex ids (original
+// variables; N - 1 for the subproblem's last vertex), with the features of the
+// learned models taken at the node's final X and the cut's final dual.
+struct NodeRecord {
+    std::vector<int> k, type, verts;   // verts: 7 per cut
+    std::vector<float> feats;          // kCutFeatures per cut
+    std::vector<double> dual;          // final dual s_c
+    std::vector<double> pred;          // warm-start dual predicted for the children (learned form)
+    size_t size() const { return k.size(); }
+};
+
+// the warm start handed to a child: the parent's record and the branching variable
+struct WarmIn {
+    std::shared_ptr<NodeRecord> rec;
+    int ic = -1;
+};
+
 struct NodeRun : CutLists {
     mcb_bab_node *node = nullptr;
     int n = 0;
@@ -73,6 +94,9 @@ struct NodeRun : CutLists {
     std::vector<double> Lsub;          // n x n subproblem matrix (host copy for the heuristic)
     std::vector<double> Zf;            // n x M factor of the last projection (times sqrt(sigma))
     std::vector<unsigned char> signs;  // Newton-Schulz form: hyperplane signs (n x N, 1 = negative)
+    std::vector<int> U;                // subproblem vertex -> original variable (n - 1 entries)
+    std::vector<float> pend_F;         // logged cut-scorer features of the last separated triangles
+    std::vector<int> pend_pos;         // ... and their positions in tri
     std::vector<int> x;                // heuristic result (BabPbSize)
     double hval = -kBig;
 };
@@ -115,6 +139,15 @@ struct mcb_ctx {
     int *d_hlist = nullptr;
     unsigned long long *d_hkeys = nullptr;
     unsigned char *d_hsign = nullptr;
+    // learned models (not owned) and the training logs
+    mcb_mlp *scorer = nullptr, *warm = nullptr;
+    std::vector<float> log_x[2], log_y[2];
+    std::map<const mcb_bab_node *, WarmIn> warm_in;           // set by the B&B driver
+    std::vector<std::shared_ptr<NodeRecord>> last_records;    // per node of the last bound_batch
+    int *d_fslot = nullptr, *d_fcp = nullptr;
+    double *d_fextra = nullptr;
+    float *d_F = nullptr, *d_pred = nullptr;
+    size_t fcap = 0;
     // instrumentation
     long long h2d = 0, d2h = 0;        // host<->device bytes moved by the bound calls
     double work[K_NCLASS] = {};        // algorithmic work per class (flops or bytes, see kWorkUnit)
@@ -492,15 +525,65 @@ void run_heuristics(mcb_ctx *c, std::vector<NodeRun *> &rs) {
         }
 }
 
+// --- learned models: features on the GPU, optional prediction ------------------
+// F (host, ncut x kCutFeatures) for cuts cps (8 ints each) of slots slot_of, and
+// pred = model(F) when a model is given
+int cut_features(mcb_ctx *c, const std::vector<int> &slot_of, const std::vector<int> &cps,
+                 const std::vector<double> *extra, mcb_mlp *model, std::vector<float> *F, std::vector<float> *pred) {
+    const size_t nc = slot_of.size();
+    if (F) F->clear();
+    if (pred) pred->clear();
+    if (nc == 0) return MCB_OK;
+    if (nc > c->fcap) {
+        void *ps[] = {c->d_fslot, c->d_fcp, c->d_fextra, c->d_F, c->d_pred};
+        for (void *q : ps)
+            if (q) cudaFree(q);
+        size_t cap = std::max<size_t>(nc, 2 * c->fcap);
+        CUDA_TRY(c, cudaMalloc(&c->d_fslot, cap * sizeof(int)));
+        CUDA_TRY(c, cudaMalloc(&c->d_fcp, cap * 8 * sizeof(int)));
+        CUDA_TRY(c, cudaMalloc(&c->d_fextra, cap * sizeof(double)));
+        CUDA_TRY(c, cudaMalloc(&c->d_F, cap * kCutFeatures * sizeof(float)));
+        CUDA_TRY(c, cudaMalloc(&c->d_pred, cap * sizeof(float)));
+        c->fcap = cap;
+    }
+    CUDA_TRY(c, h2d(c, c->d_fslot, slot_of.data(), nc * sizeof(int)));
+    CUDA_TRY(c, h2d(c, c->d_fcp, cps.data(), nc * 8 * sizeof(int)));
+    if (extra) CUDA_TRY(c, h2d(c, c->d_fextra, extra->data(), nc * sizeof(double)));
+    {
+        Prof p(c, K_LEARN, model ? 2 : 1);
+        launch_cut_features(c->d_slots, c->d_fslot, c->d_fcp, (int)nc, extra ? c->d_fextra : nullptr, c->N, c->d_F,
+                            c->st);
+        if (model) mlp_forward_device(mlp_impl(model), c->d_F, (int)nc, c->d_pred, c->st);
+    }
+    if (F) {
+        F->resize(nc * kCutFeatures);
+        CUDA_TRY(c, d2h(c, F->data(), c->d_F, F->size() * sizeof(float)));
+    }
+    if (pred && model) {
+        pred->resize(nc);
+        CUDA_TRY(c, d2h(c, pred->data(), c->d_pred, nc * sizeof(float)));
+    }
+    CUDA_TRY(c, cudaStreamSynchronize(c->st));
+    return MCB_OK;
+}
+
+void tri_key_to_cp(unsigned int key, int *cp) {
+    int t[4] = {(int)((key >> 20) & 1023), (int)((key >> 10) & 1023), (int)(key & 1023), (int)(key >> 30) + 1};
+    encode_cut(3, t, cp);
+}
+
 // --- separation --------------------------------------------------------------
 int separate_triangles(mcb_ctx *c, int ns, std::vector<NodeRun *> &runs, std::vector<int> &want) {
     int K = c->prm.TriIneq;
+    // learned ranking: the 2K most violated candidates, ranked by the scorer
+    const bool learned = (c->flags & MCB_FLAG_LEARNED) && c->scorer;
+    const int Kc = learned ? 2 * K : K;
     for (int si = 0; si < ns; ++si) c->hs[si].active = want[si];
     int rc = upload_slots(c, ns);
     if (rc) return rc;
     {
         Prof p(c, K_TRI, 6);
-        launch_tri_separation(c->d_slots, ns, c->N, c->d_trisel, c->prm.violated_TriIneq, K, c->d_tout, c->d_toutv,
+        launch_tri_separation(c->d_slots, ns, c->N, c->d_trisel, c->prm.violated_TriIneq, Kc, c->d_tout, c->d_toutv,
                               c->d_tbnd, c->d_tbndv, c->tcap_out, c->tcap_bnd, c->st);
     }
     CUDA_TRY(c, d2h(c, c->h_trisel.data(), c->d_trisel, ns * trisel_bytes()));
@@ -522,7 +605,7 @@ int separate_triangles(mcb_ctx *c, int ns, std::vector<NodeRun *> &runs, std::ve
             CUDA_TRY(c, d2h(c, pv.data(), c->d_toutv + (size_t)si * c->tcap_out, n_out * 8));
         }
         std::vector<std::pair<unsigned int, double>> sel;
-        sel.reserve(K);
+        sel.reserve(Kc);
         for (int a = 0; a < n_out; ++a) sel.push_back({pk[a], pv[a]});
         if (!take_all && n_bnd) {
             std::vector<std::pair<unsigned int, double>> b(n_bnd);
@@ -537,6 +620,23 @@ int separate_triangles(mcb_ctx *c, int ns, std::vector<NodeRun *> &runs, std::ve
             });
             for (int a = 0; a < need2 && a < n_bnd; ++a) sel.push_back(b[a]);
         }
+        if (learned && (int)sel.size() > K) {
+            std::vector<int> so(sel.size(), si), cps(sel.size() * 8);
+            for (size_t a = 0; a < sel.size(); ++a) tri_key_to_cp(sel[a].first, &cps[8 * a]);
+            std::vector<float> pred;
+            int rc2 = cut_features(c, so, cps, nullptr, c->scorer, nullptr, &pred);
+            if (rc2) return rc2;
+            std::vector<int> ord(sel.size());
+            for (size_t a = 0; a < ord.size(); ++a) ord[a] = (int)a;
+            std::stable_sort(ord.begin(), ord.end(), [&](int x, int y) {
+                if (pred[x] != pred[y]) return pred[x] > pred[y];
+                if (sel[x].second != sel[y].second) return sel[x].second > sel[y].second;
+                return sel[x].first < sel[y].first;
+            });
+            std::vector<std::pair<unsigned int, double>> top;
+            for (int a = 0; a < K; ++a) top.push_back(sel[ord[a]]);
+            sel.swap(top);
+        }
         std::sort(sel.begin(), sel.end());
         // updateTriangleInequalities, cutting_planes.c:132-214 (purge already done by the caller)
         std::unordered_set<uint64_t> have;
@@ -546,13 +646,29 @@ int separate_triangles(mcb_ctx *c, int ns, std::vector<NodeRun *> &runs, std::ve
             have.insert(((uint64_t)(t[3] - 1) << 30) | ((uint64_t)t[0] << 20) | ((uint64_t)t[1] << 10) | (uint64_t)t[2]);
         }
         size_t next = r.tri.size() / 4;
+        const size_t first_new = next;
+        std::vector<int> so, cps;
         for (auto &e : sel) {
             if (next == MCB_MAX_TRI) break;
             if (have.count(e.first)) continue;
             int type = (int)(e.first >> 30) + 1, i = (e.first >> 20) & 1023, j = (e.first >> 10) & 1023, k = e.first & 1023;
             r.tri.insert(r.tri.end(), {i, j, k, type});
             r.tri_y.push_back(0.0);
+            if (c->flags & MCB_FLAG_LOG) {
+                so.push_back(si);
+                cps.resize(cps.size() + 8);
+                tri_key_to_cp(e.first, &cps[cps.size() - 8]);
+            }
             ++next;
+        }
+        if ((c->flags & MCB_FLAG_LOG) && !so.empty()) {
+            // features at separation time; the targets are the duals after the next ADMM call
+            std::vector<float> F;
+            int rc2 = cut_features(c, so, cps, nullptr, nullptr, &F, nullptr);
+            if (rc2) return rc2;
+            r.pend_F = F;
+            r.pend_pos.clear();
+            for (size_t a = 0; a < so.size(); ++a) r.pend_pos.push_back((int)(first_new + a));
         }
         r.viol3 = maxv;
     }
@@ -674,6 +790,20 @@ int separate_kgonal(mcb_ctx *c, int ns, std::vector<NodeRun *> &runs, std::vecto
     return MCB_OK;
 }
 
+// training pairs of the cut scorer: features at separation -> log(1 + dual after the ADMM call)
+void log_scorer_targets(mcb_ctx *c, NodeRun &r, const std::vector<double> &s) {
+    if (!(c->flags & MCB_FLAG_LOG)) return;
+    for (size_t a = 0; a < r.pend_pos.size(); ++a) {
+        size_t pos = (size_t)r.pend_pos[a];
+        if (pos >= s.size()) continue;
+        c->log_x[0].insert(c->log_x[0].end(), r.pend_F.begin() + a * kCutFeatures,
+                           r.pend_F.begin() + (a + 1) * kCutFeatures);
+        c->log_y[0].push_back((float)log1p(std::max(s[pos], 0.0)));
+    }
+    r.pend_F.clear();
+    r.pend_pos.clear();
+}
+
 // purge cuts whose dual s is below 1e-5 (cutting_planes.c:144-166 and analogues)
 void purge(NodeRun &r, const std::vector<double> &s) {
     size_t nt = r.tri.size() / 4, np = r.pent.size() / 6, nh = r.hept.size() / 8;
@@ -755,6 +885,85 @@ int ns_hyperplanes(mcb_ctx *c, std::vector<NodeRun *> &runs, std::vector<NodeRun
     return MCB_OK;
 }
 
+// the parent's final cuts mapped into the child's subproblem (cuts through the
+// branching variable dropped), with the warm model's predicted duals as y0
+void apply_warm_start(mcb_ctx *c, NodeRun &r) {
+    auto it = c->warm_in.find(r.node);
+    if (it == c->warm_in.end() || !it->second.rec) return;
+    const NodeRecord &P = *it->second.rec;
+    if (P.pred.size() != P.size()) return;
+    std::vector<int> loc(c->N, -1);
+    for (size_t v = 0; v < r.U.size(); ++v) loc[r.U[v]] = (int)v;
+    loc[c->N - 1] = r.n - 1;
+    for (size_t q = 0; q < P.size(); ++q) {
+        const int k = P.k[q];
+        int v[7];
+        bool ok = true;
+        for (int a = 0; a < k && ok; ++a) {
+            v[a] = loc[P.verts[7 * q + a]];
+            ok = v[a] >= 0;
+        }
+        double y0 = expm1(std::max((double)P.pred[q], 0.0));
+        if (!ok || y0 < 1e-5) continue;
+        if (k == 3) {
+            if ((int)(r.tri.size() / 4) >= MCB_MAX_TRI) continue;
+            r.tri.insert(r.tri.end(), {v[0], v[1], v[2], P.type[q]});
+            r.tri_y.push_back(y0);
+        } else if (k == 5) {
+            if ((int)(r.pent.size() / 6) >= MCB_MAX_PENT) continue;
+            r.pent.push_back(P.type[q]);
+            r.pent.insert(r.pent.end(), v, v + 5);
+            r.pent_y.push_back(y0);
+        } else {
+            if ((int)(r.hept.size() / 8) >= MCB_MAX_HEPT) continue;
+            r.hept.push_back(P.type[q]);
+            r.hept.insert(r.hept.end(), v, v + 7);
+            r.hept_y.push_back(y0);
+        }
+    }
+}
+
+// the node's final record (cuts with dual >= 1e-5 of its last ADMM call, features
+// at its final X, the warm model's predictions when loaded)
+int make_record(mcb_ctx *c, int si, NodeRun &r, std::shared_ptr<NodeRecord> &out) {
+    out = std::make_shared<NodeRecord>();
+    const int m = r.m();
+    if (m == 0 || r.count == 0) return MCB_OK;
+    std::vector<double> sv(m);
+    CUDA_TRY(c, d2h(c, sv.data(), c->hs[si].s, m * sizeof(double)));
+    log_scorer_targets(c, r, sv);
+    NodeRecord &R = *out;
+    std::vector<int> so, cps;
+    std::vector<double> ex;
+    auto glob = [&](int v) { return v == r.n - 1 ? c->N - 1 : r.U[v]; };
+    auto add = [&](int k, int type, const int *v, double dual) {
+        R.k.push_back(k);
+        R.type.push_back(type);
+        for (int a = 0; a < 7; ++a) R.verts.push_back(a < k ? glob(v[a]) : 0);
+        R.dual.push_back(dual);
+        int cp[8], raw[8];
+        if (k == 3) { raw[0] = v[0]; raw[1] = v[1]; raw[2] = v[2]; raw[3] = type; }
+        else { raw[0] = type; for (int a = 0; a < k; ++a) raw[1 + a] = v[a]; }
+        encode_cut(k, raw, cp);
+        so.push_back(si);
+        cps.insert(cps.end(), cp, cp + 8);
+        ex.push_back(dual);
+    };
+    size_t q = 0;
+    for (size_t a = 0; a < r.tri.size() / 4; ++a, ++q)
+        if (sv[q] >= 1e-5) add(3, r.tri[4 * a + 3], &r.tri[4 * a], sv[q]);
+    for (size_t a = 0; a < r.pent.size() / 6; ++a, ++q)
+        if (sv[q] >= 1e-5) add(5, r.pent[6 * a], &r.pent[6 * a + 1], sv[q]);
+    for (size_t a = 0; a < r.hept.size() / 8; ++a, ++q)
+        if (sv[q] >= 1e-5) add(7, r.hept[8 * a], &r.hept[8 * a + 1], sv[q]);
+    std::vector<float> pred;
+    mcb_mlp *model = (c->flags & MCB_FLAG_LEARNED) ? c->warm : nullptr;
+    int rc = cut_features(c, so, cps, &ex, model, &R.feats, model ? &pred : nullptr);
+    if (rc) return rc;
+    if (model) R.pred.assign(pred.begin(), pred.end());
+    return MCB_OK;
+}
+
 // --- the batched SDPbound ----------------------------------------------------
 int bound_batch(mcb_ctx *c, mcb_bab_node *const *nodes, int count, int rank, double *bounds, mcb_node_stats *stats) {
     auto t0 = std::chrono::steady_clock::now();
@@ -785,6 +994,7 @@ int bound_batch(mcb_ctx *c, mcb_bab_node *const *nodes, int count, int rank, dou
         for (int v : FX) *p++ = v;
         for (int v : FS) *p++ = v;
         r.n = (int)U.size() + 1;
+        r.U = U;
         r.key = node_key(r.node->xfixed, r.node->sol, pb);
         r.sigma = P.sigma0;
         r.tol = P.tol0;
@@ -838,6 +1048,9 @@ int bound_batch(mcb_ctx *c, mcb_bab_node *const *nodes, int count, int rank, dou
         if (P.use_diff && rank != 0 && r.bound > c->LB + c->diff + 1.0) { r.giveup = 1; r.done = 1; continue; }
         want[si] = 1;
     }
+    if ((c->flags & MCB_FLAG_LEARNED) && c->warm)
+        for (int si = 0; si < ns; ++si)
+            if (want[si]) apply_warm_start(c, R[si]);
     if ((rc = separate_triangles(c, ns, runs, want))) return rc;
     for (int si = 0; si < ns; ++si)
         if (want[si]) R[si].sep_round++;
@@ -965,6 +1178,7 @@ int bound_batch(mcb_ctx *c, mcb_bab_node *const *nodes, int count, int rank, dou
             sbuf.resize(r.m());
             if (!sbuf.empty())
                 CUDA_TRY(c, d2h(c, sbuf.data(), c->hs[si].s, sbuf.size() * sizeof(double)));
+            log_scorer_targets(c, r, sbuf);
             purge(r, sbuf);
         }
         if (std::any_of(want3.begin(), want3.end(), [](int v) { return v; }))
@@ -1009,6 +1223,12 @@ int bound_batch(mcb_ctx *c, mcb_bab_node *const *nodes, int count, int rank, dou
             store_fracsol(c, r, row);
         }
     }
+    const bool want_records = (c->flags & MCB_FLAG_LOG) || ((c->flags & MCB_FLAG_LEARNED) && c->warm);
+    c->last_records.assign(ns, nullptr);
+    if (want_records)
+        for (int si = 0; si < ns; ++si)
+            if (!R[si].status && !R[si].prune)
+                if ((rc = make_record(c, si, R[si], c->last_records[si]))) return rc;
     flush_prof(c);
     int ret = MCB_OK;
     double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
@@ -1101,7 +1321,7 @@ mcb_ctx *mcb_create(const mcb_params *params, int N, const double *SL, int batch
     if (rc == MCB_OK) chk(cudaMalloc(&c->d_fixed, batch_max * sizeof(double)));
     if (rc == MCB_OK) chk(cudaMalloc(&c->d_trisel, batch_max * trisel_bytes()));
     c->h_trisel.resize(batch_max * trisel_bytes());
-    c->tcap_out = c->prm.TriIneq + 16;
+    c->tcap_out = 2 * c->prm.TriIneq + 16;  // the learned ranking reads 2K candidates
     c->tcap_bnd = 1 << 16;
     if (rc == MCB_OK) chk(cudaMalloc(&c->d_tout, (size_t)batch_max * c->tcap_out * sizeof(unsigned int)));
     if (rc == MCB_OK) chk(cudaMalloc(&c->d_toutv, (size_t)batch_max * c->tcap_out * sizeof(double)));
@@ -1131,7 +1351,7 @@ void mcb_destroy(mcb_ctx *c) {
     c->ns.destroy();
     void *ps[] = {c->d_SL, c->d_slots, c->d_partials, c->d_lists, c->d_fixed, c->d_trisel, c->d_tout, c->d_toutv,
                   c->d_tbnd, c->d_tbndv, c->d_sajobs, c->d_perm, c->d_saout, c->d_saval,
-                  c->d_hlist, c->d_hkeys, c->d_hsign};
+                  c->d_hlist, c->d_hkeys, c->d_hsign, c->d_fslot, c->d_fcp, c->d_fextra, c->d_F, c->d_pred};
     for (void *p : ps)
         if (p) cudaFree(p);
     for (auto &p : c->pending) { cudaEventDestroy(p.second.first); cudaEventDestroy(p.second.second); }
@@ -1150,6 +1370,30 @@ double mcb_get_lb(const mcb_ctx *c, int *sol) {
 }
 void mcb_set_diff(mcb_ctx *c, double d) { c->diff = d; }
 double mcb_get_diff(const mcb_ctx *c) { return c->diff; }
+int mcb_set_models(mcb_ctx *c, mcb_mlp *scorer, mcb_mlp *warm) {
+    if (!c) return MCB_ERR_ARG;
+    if ((scorer && mcb_mlp_num_params(scorer) <= 0) || (warm && mcb_mlp_num_params(warm) <= 0)) return MCB_ERR_ARG;
+    if ((scorer && mlp_inputs(scorer) != kCutFeatures) || (warm && mlp_inputs(warm) != kCutFeatures))
+        return MCB_ERR_ARG;
+    c->scorer = scorer;
+    c->warm = warm;
+    return MCB_OK;
+}
+int mcb_log_count(const mcb_ctx *c, int which) {
+    if (!c || which < 0 || which > 1) return 0;
+    return (int)c->log_y[which].size();
+}
+int mcb_log_fetch(const mcb_ctx *c, int which, int cap, float *X, float *y) {
+    if (!c || which < 0 || which > 1) return MCB_ERR_ARG;
+    int k = std::min(cap, (int)c->log_y[which].size());
+    if (X) memcpy(X, c->log_x[which].data(), (size_t)k * kCutFeatures * sizeof(float));
+    if (y) memcpy(y, c->log_y[which].data(), (size_t)k * sizeof(float));
+    return k;
+}
+void mcb_log_clear(mcb_ctx *c) {
+    if (!c) return;
+    for (int w = 0; w < 2; ++w) { c->log_x[w].clear(); c->log_y[w].clear(); }
+}
 int mcb_ns_options(mcb_ctx *c, int operands, double l0) {
     if (!c || c->proj == MCB_PROJ_FP64) return MCB_ERR_ARG;
     return c->ns.configure(operands, l0);
@@ -1234,6 +1478,30 @@ mcb_bab_node *child_of(const mcb_bab_node *p, int pb, int ic, int xic) {
     return n;
 }
 
+// training pairs of the warm-start model: the parent's cut features (with its dual)
+// -> log(1 + the same cut's dual at the end of the child's cold-started bound)
+void log_warm_pairs(mcb_ctx *c, const WarmIn &w, const std::shared_ptr<NodeRecord> &child) {
+    if (!w.rec || !child || child->size() == 0) return;
+    std::map<std::vector<int>, double> cd;
+    for (size_t q = 0; q < child->size(); ++q) {
+        std::vector<int> key{child->k[q], child->type[q]};
+        key.insert(key.end(), child->verts.begin() + 7 * q, child->verts.begin() + 7 * q + child->k[q]);
+        cd[key] = child->dual[q];
+    }
+    const NodeRecord &P = *w.rec;
+    for (size_t q = 0; q < P.size(); ++q) {
+        bool through = false;
+        for (int a = 0; a < P.k[q]; ++a) through = through || P.verts[7 * q + a] == w.ic;
+        if (through) continue;
+        std::vector<int> key{P.k[q], P.type[q]};
+        key.insert(key.end(), P.verts.begin() + 7 * q, P.verts.begin() + 7 * q + P.k[q]);
+        auto it = cd.find(key);
+        double t = it == cd.end() ? 0.0 : it->second;
+        c->log_x[1].insert(c->log_x[1].end(), P.feats.begin() + q * kCutFeatures, P.feats.begin() + (q + 1) * kCutFeatures);
+        c->log_y[1].push_back((float)log1p(std::max(t, 0.0)));
+    }
+}
+
 int branching_var(const mcb_ctx *c, const mcb_bab_node *node) {
     int ic = -1;
     if (c->prm.branchingStrategy == 0) {
@@ -1265,7 +1533,13 @@ int mcb_bab(mcb_ctx *c, int batch, int max_nodes, double *opt, int *sol, double 
     root->upper_bound = rb;
     if (rc == MCB_OK && c->LB + 1.0 < rb && !c->prm.root) {
         int ic = branching_var(c, root);
-        for (int xic = 0; xic <= 1 && ic >= 0; ++xic) { h.push(child_of(root, c->pb, ic, xic)); nodes++; }
+        std::shared_ptr<NodeRecord> rec = c->last_records.empty() ? nullptr : c->last_records[0];
+        for (int xic = 0; xic <= 1 && ic >= 0; ++xic) {
+            mcb_bab_node *ch = child_of(root, c->pb, ic, xic);
+            if (rec && rec->size()) c->warm_in[ch] = WarmIn{rec, ic};
+            h.push(ch);
+            nodes++;
+        }
     }
     free(root);
     std::vector<mcb_bab_node *> cur;
@@ -1282,10 +1556,20 @@ int mcb_bab(mcb_ctx *c, int batch, int max_nodes, double *opt, int *sol, double 
         for (size_t a = 0; a < cur.size(); ++a) {
             if (log && lc < log_cap) log[lc++] = sts[a];
             cur[a]->upper_bound = b[a];
+            std::shared_ptr<NodeRecord> rec = a < c->last_records.size() ? c->last_records[a] : nullptr;
+            auto it = c->warm_in.find(cur[a]);
+            if (it != c->warm_in.end()) {
+                if (c->flags & MCB_FLAG_LOG) log_warm_pairs(c, it->second, rec);
+                c->warm_in.erase(it);
+            }
             if (rc == MCB_OK && c->LB + 1.0 < b[a]) {
                 int ic = branching_var(c, cur[a]);
                 if (ic >= 0) {
-                    for (int xic = 0; xic <= 1; ++xic) h.push(child_of(cur[a], c->pb, ic, xic));
+                    for (int xic = 0; xic <= 1; ++xic) {
+                        mcb_bab_node *ch = child_of(cur[a], c->pb, ic, xic);
+                        if (rec && rec->size()) c->warm_in[ch] = WarmIn{rec, ic};
+                        h.push(ch);
+                    }
                     nodes += 2;
                 }
             }
@@ -1293,6 +1577,7 @@ int mcb_bab(mcb_ctx *c, int batch, int max_nodes, double *opt, int *sol, double 
         }
     }
     for (auto *n : h.d) free(n);
+    c->warm_in.clear();
     if (opt) *opt = c->LB;
     if (sol) memcpy(sol, c->best_sol.data(), c->pb * sizeof(int));
     if (nodes_out) *nodes_out = nodes;

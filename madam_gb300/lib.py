@@ -23,7 +23,9 @@ NS_OPERANDS_NATIVE, NS_OPERANDS_SPLIT, NS_OPERANDS_FP32 = 0, 1, 2
 def PROJ_OPERANDS(op):
     """Operand choice of the Newton-Schulz forms for `project` (MCB_PROJ_OPERANDS)."""
     return (op + 1) << 4
-FLAG_PROFILE, FLAG_LEARNED = 0x100, 0x200
+FLAG_PROFILE, FLAG_LEARNED, FLAG_LOG = 0x100, 0x200, 0x400
+CUT_FEATURES = 10
+LOG_SCORER, LOG_WARM = 0, 1
 
 PARAM_FIELDS = [
     ("sigma0", C.c_double), ("scaleSigma", C.c_double), ("ADMM_itermax", C.c_int),
@@ -129,6 +131,20 @@ def lib():
     L.mcb_measure_fp64_peak.restype = C.c_double
     L.mcb_ns_options.argtypes = [C.c_void_p, C.c_int, C.c_double]
     L.mcb_ns_schedule.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+    L.mcb_mlp_create.restype = C.c_void_p
+    L.mcb_mlp_create.argtypes = [C.c_int, C.c_int, C.c_int, C.c_uint64, C.POINTER(C.c_int)]
+    L.mcb_mlp_destroy.argtypes = [C.c_void_p]
+    L.mcb_mlp_num_params.argtypes = [C.c_void_p]
+    L.mcb_mlp_get_params.argtypes = [C.c_void_p, C.c_void_p]
+    L.mcb_mlp_set_params.argtypes = [C.c_void_p, C.c_void_p]
+    L.mcb_mlp_predict.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]
+    L.mcb_mlp_gradient.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
+    L.mcb_mlp_train.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_float,
+                                C.c_uint64, C.c_void_p]
+    L.mcb_set_models.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+    L.mcb_log_count.argtypes = [C.c_void_p, C.c_int]
+    L.mcb_log_fetch.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p]
+    L.mcb_log_clear.argtypes = [C.c_void_p]
     L.mcb_launch_count.restype = C.c_longlong
     L.mcb_launch_count.argtypes = [C.c_void_p]
     _lib = L
@@ -239,6 +255,22 @@ class Context:
         lib().mcb_transfer_stats(self.h, C.byref(a), C.byref(b))
         return a.value, b.value
 
+    def set_models(self, scorer=None, warm=None):
+        """Attach learned models (MLP objects; kept alive by the context)."""
+        self._models = (scorer, warm)
+        _check(lib().mcb_set_models(self.h, scorer.h if scorer else None, warm.h if warm else None), self.h)
+
+    def log(self, which):
+        k = lib().mcb_log_count(self.h, which)
+        X = np.zeros((k, CUT_FEATURES), dtype=np.float32)
+        y = np.zeros(k, dtype=np.float32)
+        if k:
+            lib().mcb_log_fetch(self.h, which, k, X.ctypes.data, y.ctypes.data)
+        return X, y
+
+    def clear_log(self):
+        lib().mcb_log_clear(self.h)
+
     def ns_options(self, operands=NS_OPERANDS_SPLIT, l0=1e-6):
         _check(lib().mcb_ns_options(self.h, operands, l0), self.h)
 
@@ -253,6 +285,63 @@ class Context:
 
     def launch_count(self):
         return lib().mcb_launch_count(self.h)
+
+
+class MLP:
+    """The learned models' network, trained and evaluated by the library's own kernels."""
+
+    def __init__(self, d_in, h1=32, h2=32, seed=0):
+        st = C.c_int()
+        self.d, self.h1, self.h2 = d_in, h1, h2
+        self.h = lib().mcb_mlp_create(d_in, h1, h2, seed, C.byref(st))
+        if not self.h:
+            _check(st.value)
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().mcb_mlp_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def num_params(self):
+        return lib().mcb_mlp_num_params(self.h)
+
+    def params(self):
+        p = np.zeros(self.num_params(), dtype=np.float32)
+        _check(lib().mcb_mlp_get_params(self.h, p.ctypes.data))
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        assert p.size == self.num_params()
+        _check(lib().mcb_mlp_set_params(self.h, p.ctypes.data))
+
+    def predict(self, X):
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        out = np.zeros(len(X), dtype=np.float32)
+        _check(lib().mcb_mlp_predict(self.h, X.ctypes.data, len(X), out.ctypes.data))
+        return out
+
+    def gradient(self, X, Y):
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        Y = np.ascontiguousarray(Y, dtype=np.float32)
+        g = np.zeros(self.num_params(), dtype=np.float32)
+        loss = C.c_float()
+        _check(lib().mcb_mlp_gradient(self.h, X.ctypes.data, Y.ctypes.data, len(X), g.ctypes.data, C.byref(loss)))
+        return float(loss.value), g
+
+    def train(self, X, Y, epochs=50, batch=256, lr=3e-3, seed=0):
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        Y = np.ascontiguousarray(Y, dtype=np.float32)
+        loss = C.c_float()
+        _check(lib().mcb_mlp_train(self.h, X.ctypes.data, Y.ctypes.data, len(X), epochs, batch, lr, seed,
+                                   C.byref(loss)))
+        return float(loss.value)
 
 
 def fp64_peak_gflops():

@@ -179,3 +179,22 @@ def test_create_subproblem_against_numpy(orc):
     fv = orc.fixed_value(SL.ravel(order="F"), n, xf, so)
     x = np.array([so[i] if xf[i] else 0 for i in range(n - 1)], float)
     assert abs(fv - x @ Lap @ x) < 1e-9
+
+
+def test_mlp_restatement_gradient_against_finite_differences():
+    from oracle import mlp_ref as R
+
+    rng = np.random.default_rng(0)
+    d, h1, h2 = 6, 5, 4
+    P = h1 * d + h1 + h2 * h1 + 2 * h2 + 1
+    p = rng.standard_normal(P) * 0.5
+    X = rng.standard_normal((20, d))
+    Y = rng.standard_normal(20)
+    _, g = R.loss_and_grad(p, X, Y, d, h1, h2)
+    eps = 1e-6
+    num = np.zeros(P)
+    for q in range(P):
+        e = np.zeros(P)
+        e[q] = eps
+        num[q] = (R.loss_and_grad(p + e, X, Y, d, h1, h2)[0] - R.loss_and_grad(p - e, X, Y, d, h1, h2)[0]) / (2 * eps)
+    assert np.allclose(g, num, rtol=1e-6, atol=1e-8)
