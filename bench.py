@@ -5,12 +5,17 @@ One step = one batched call that bounds a whole batch of branch-and-bound
 nodes (IPM + cutting-plane ADMM rounds + separations + safe bound per node) of
 the configured workload; the problem matrix is resident on the device.
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME]
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME] [--form F]
   python bench.py --impl reference ...   # the reference's CPU method on the host cores
 
-Prints one JSON line (rank 0).  `value` is node bounds per second over the
-device-timed region (CUDA events on the library's stream); `e2e` is the same
-through the C ABI call with host buffers, timed on the host.
+Forms: "learned" (default: Newton-Schulz projection on the tensor cores plus the
+shipped learned cut ranking / warm start), "mixed" (Newton-Schulz only), "fp64"
+(the plain method).  Prints one JSON line (rank 0).  `value` is node bounds per
+second of the chosen form over the device-timed region (CUDA events on the
+library's stream); `e2e` is the same through the C ABI call with host buffers,
+timed on the host; `plain_fp64` is the plain form on the same workload in the
+same run, and `time_to_optimum` a full branch-and-bound of a seeded G(100, 0.5)
+unit-weight instance (triangle cuts) in both forms.
 """
 import argparse
 import json
@@ -36,7 +41,8 @@ def _args():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="gnp256_pm1_batch64")
-    ap.add_argument("--proj", default="fp64", choices=["fp64"])
+    ap.add_argument("--form", default="learned", choices=["learned", "mixed", "fp64"])
+    ap.add_argument("--no-compare", action="store_true", help="skip the plain-form and time-to-optimum legs")
     ap.add_argument("--cpu-sample", type=int, default=0, help="nodes in the CPU sample (0: one per core)")
     ap.add_argument("--cpu-only", action="store_true", help=argparse.SUPPRESS)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -148,6 +154,80 @@ def measured_peaks():
 
 
 # ---------------------------------------------------------------------------
+FORMS = {"learned": "Newton-Schulz projection (BF16 split operands, FP64 product) + learned cut ranking and warm start",
+         "mixed": "Newton-Schulz projection (BF16 split operands, FP64 product)",
+         "fp64": "plain FP64 tridiagonal eigensolver"}
+TTO = dict(n=100, p=0.5, weights="one", seed=1101, params=dict(include_Pent=0, include_Hepta=0))
+
+
+def _context(M, prm, SL, n, batch, form, stream=None, profile=True):
+    flags = M.PROJ_FP64 if form == "fp64" else M.PROJ_NS_BF16
+    if form == "learned":
+        flags |= M.FLAG_LEARNED
+    if profile:
+        flags |= M.FLAG_PROFILE
+    ctx = M.Context(prm, SL, n, batch_max=batch, flags=flags, stream=stream)
+    if form == "learned":
+        from madam_gb300 import learn as L
+        from madam_gb300 import train_models as T
+
+        ctx.set_models(*L.load(T.OUT))
+    return ctx
+
+
+def _time_steps(torch, ctx, step, stream, steps, warmup, dist=None, clocks=None):
+    for _ in range(warmup):
+        step()
+    torch.cuda.synchronize()
+    ctx.reset_kernel_stats()
+    if dist:
+        dist.barrier()
+    if clocks:
+        clocks.start()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ev0.record(stream)
+    stats = []
+    for _ in range(steps):
+        stats.append(step())
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    if dist:
+        dist.barrier()
+    clk = clocks.stop() if clocks else None
+    return ev0.elapsed_time(ev1) / 1e3, wall, stats, clk
+
+
+def _roofline(M, ks, kw):
+    """Achieved rate of the dominant kernel class with counted work, against the measured peak."""
+    peaks = measured_peaks()
+    counted = {k: v for k, v in ks.items() if kw.get(k, (0, 0))[1] and v[1] > 0}
+    if not counted:
+        return None
+    name, (nl, ms) = max(counted.items(), key=lambda kv: kv[1][1])
+    work, unit = kw[name]
+    base = {"kernel": name, "launches": nl, "ms_total": ms, "traffic": None}
+    if unit == 1:
+        peak = M.fp64_peak_gflops() / 1e3
+        ach = work / (ms / 1e3) / 1e12
+        base.update(bound="fp64", achieved=ach, peak=peak, unit="TFLOP/s", frac=ach / peak,
+                    peak_source="measured FP64 FMA microbenchmark (no FP64 entry in the measured peaks file)")
+    elif unit == 2:
+        hbm = peaks.get("hbm_gbs", 6800.0)
+        ach = work / (ms / 1e3) / 1e9
+        base.update(bound="hbm", achieved=ach, peak=hbm, unit="GB/s", frac=ach / hbm,
+                    peak_source="measured" if "hbm_gbs" in peaks else "fallback")
+    else:
+        bf = peaks.get("bf16_tflops", 1900.0)
+        ach = work / (ms / 1e3) / 1e12
+        base.update(bound="tensor", achieved=ach, peak=bf, unit="TFLOP/s", frac=ach / bf,
+                    peak_source=("measured" if "bf16_tflops" in peaks else "fallback") + " dense BF16 burst; "
+                    "the work counts each split-operand GEMM once (2 n^3), not its BF16 passes")
+    return base
+
+
 def run_ours(a):
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -161,6 +241,7 @@ def run_ours(a):
         dist.init_process_group("nccl")
     import torch
 
+    from madam_gb300 import graphs as G
     from madam_gb300 import lib as M
     from madam_gb300 import workload as W
 
@@ -170,47 +251,26 @@ def run_ours(a):
     nodes_fix = wl["fixings"]
     batch = len(nodes_fix)
     prm = M.params(**wl["params"])
-    ctx = M.Context(prm, wl["SL"], wl["n"], batch_max=batch, flags=M.PROJ_FP64 | M.FLAG_PROFILE,
-                    stream=stream.cuda_stream)
-
     base_trials = (prm.Pent_Trials, prm.Hepta_Trials)
 
-    def step():
-        # every step starts from the same state: incumbent and the Pent/Hepta_Trials
-        # that give-ups grow (bounding.c:184-187) reset
-        ctx.set_trials(*base_trials)
-        ctx.set_lb(wl["lb"], wl["lb_sol"])
-        nodes = [M.node(f) for f in nodes_fix]
-        b, st = ctx.bound_batch(nodes, rank=1)
-        return b, st
+    def make_step(ctx):
+        def step():
+            # every step starts from the same state: incumbent and the Pent/Hepta_Trials
+            # that give-ups grow (bounding.c:184-187) reset
+            ctx.set_trials(*base_trials)
+            ctx.set_lb(wl["lb"], wl["lb_sol"])
+            nodes = [M.node(f) for f in nodes_fix]
+            return ctx.bound_batch(nodes, rank=1)[1]
+        return step
 
-    for _ in range(a.warmup):
-        step()
-    torch.cuda.synchronize()
-    ctx.reset_kernel_stats()
-    if dist:
-        dist.barrier()
-    clocks = Clocks(local)
-    clocks.start()
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    ev0.record(stream)
-    stats = []
-    for _ in range(a.steps):
-        b, st = step()
-        stats.append(st)
-    ev1.record(stream)
-    torch.cuda.synchronize()
-    wall = time.perf_counter() - t0
-    if dist:
-        dist.barrier()
-    clk = clocks.stop()
-    dev_s = ev0.elapsed_time(ev1) / 1e3
+    ctx = _context(M, prm, wl["SL"], wl["n"], batch, a.form, stream.cuda_stream)
+    dev_s, wall, stats, clk = _time_steps(torch, ctx, make_step(ctx), stream, a.steps, a.warmup, dist, Clocks(local))
     launches = ctx.launch_count()
+    lib_launches = ctx.library_launch_count()
     ks = ctx.kernel_stats()
     kw = ctx.kernel_work()
     h2d, d2h = ctx.transfer_stats()
+    ctx.close()
     if dist:
         t = torch.tensor([dev_s, wall], device="cuda", dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -219,29 +279,32 @@ def run_ours(a):
     if rank != 0:
         dist.destroy_process_group()
         return
-    # roofline of the dominant kernel class
-    fp64_peak = M.fp64_peak_gflops()
-    peaks = measured_peaks()
-    dom = max(ks.items(), key=lambda kv: kv[1][1])
-    counted = {k: v for k, v in ks.items() if kw.get(k, (0, 0))[1] and v[1] > 0}
-    roof = None
-    name, (nl, ms) = dom
-    work, unit = kw.get(name, (0.0, 0))
-    if not unit and counted:
-        name, (nl, ms) = max(counted.items(), key=lambda kv: kv[1][1])
-        work, unit = kw[name]
-    if unit == 1:
-        ach = work / (ms / 1e3) / 1e12
-        roof = {"kernel": name, "bound": "fp64", "achieved": ach, "peak": fp64_peak / 1e3, "unit": "TFLOP/s",
-                "frac": ach / (fp64_peak / 1e3), "traffic": None, "launches": nl, "ms_per_launch": ms / max(nl, 1),
-                "peak_source": "measured FP64 FMA microbenchmark (no FP64 entry in the measured peaks file)"}
-    elif unit == 2:
-        hbm = peaks.get("hbm_gbs", 6800.0)
-        ach = work / (ms / 1e3) / 1e9
-        roof = {"kernel": name, "bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
-                "traffic": None, "launches": nl, "ms_per_launch": ms / max(nl, 1),
-                "peak_source": "measured" if "hbm_gbs" in peaks else "fallback"}
-    share = {k: round(v[1] / max(1e-9, sum(x[1] for x in ks.values())), 4) for k, v in ks.items() if v[0]}
+    roof = _roofline(M, ks, kw)
+    tot_ms = sum(x[1] for x in ks.values())
+    share = {k: round(v[1] / max(1e-9, tot_ms), 4) for k, v in ks.items() if v[1] > 0}
+    plain = tto = None
+    if not a.no_compare and a.form != "fp64":
+        # the plain FP64 form on the same workload (one warm-up, one timed step)
+        pc = _context(M, prm, wl["SL"], wl["n"], batch, "fp64", stream.cuda_stream)
+        pd, pw, pst, _ = _time_steps(torch, pc, make_step(pc), stream, 1, 1)
+        pc.close()
+        plain = {"value": batch / pd, "unit": UNIT, "ms_per_step": pd * 1e3, "steps": 1, "warmup": 1,
+                 "admm_iters_per_step": sum(s.admm_iters for s in pst[0])}
+        # time to proven optimum, both forms
+        n, e, w = G.gnp(TTO["n"], TTO["p"], TTO["weights"], seed=TTO["seed"])
+        SLt = G.extended_laplacian(n, e, w).ravel(order="F")
+        tto = {"instance": "G(%d, %.1f) %s weights seed %d, triangle cuts, batch 64" % (
+            TTO["n"], TTO["p"], TTO["weights"], TTO["seed"])}
+        for form in (a.form, "fp64"):
+            tc = _context(M, M.params(**TTO["params"]), SLt, n, 64, form, profile=False)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            r = tc.bab(batch=64, max_nodes=20000)
+            tto[form] = {"seconds": time.perf_counter() - t0, "optimum": r["opt"], "nodes": r["nodes"],
+                         "root_bound": r["root_bound"]}
+            tc.close()
+        tto["speedup"] = tto["fp64"]["seconds"] / tto[a.form]["seconds"]
+        tto["same_optimum"] = tto["fp64"]["optimum"] == tto[a.form]["optimum"]
     cpu = None
     if not a.no_cpu_baseline:
         cores = host_cores()
@@ -259,8 +322,10 @@ def run_ours(a):
     out = {
         "metric": METRIC, "value": total_nodes / dev_s, "unit": UNIT, "n_gpus": world, "steps": a.steps,
         "warmup": a.warmup, "ms_per_step": dev_s * 1e3 / a.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded rudy-style G(n,p) graph and node fixings)",
-        "config": {"workload": a.workload, "n": wl["n"], "nodes_per_step": batch, "projection": "fp64 eigensolver",
+        "vs_baseline": None, "dtype": "f64" if a.form == "fp64" else "bf16 split (FP32-accurate) + f64",
+        "data": "synthetic (seeded rudy-style G(n,p) graph and node fixings)",
+        "config": {"workload": a.workload, "n": wl["n"], "nodes_per_step": batch, "form": a.form,
+                   "projection": FORMS[a.form],
                    "cuts": "tri+pent" if not wl["params"].get("include_Hepta", 1) else "tri+pent+hept",
                    "params": "reference shipped params file, " + ", ".join("%s=%s" % kv for kv in wl["params"].items()),
                    "incumbent": wl["lb"], "l2": "working set per step > L2 (64 nodes x 8 n^2 FP64 buffers)",
@@ -268,9 +333,13 @@ def run_ours(a):
         "e2e": {"value": total_nodes / wall, "unit": UNIT, "h2d_bytes_per_step": h2d // a.steps,
                 "d2h_bytes_per_step": d2h // a.steps},
         "gpu_launches": launches,
+        "library_launches": lib_launches,
         "roofline": roof,
         "kernel_time_share": share,
         "admm_iters_per_step": admm // a.steps,
+        "plain_fp64": plain,
+        "speedup_vs_plain_fp64": (plain["ms_per_step"] / (dev_s * 1e3 / a.steps)) if plain else None,
+        "time_to_optimum": tto,
         "cpu_baseline": cpu,
         "clocks": clk,
     }

@@ -50,8 +50,9 @@ enum mcb_status {
 #define MCB_FLAG_PROFILE 0x100 /* time every kernel class with CUDA events */
 /* operands of the Newton-Schulz growth steps (mcb_ns_options) */
 #define MCB_NS_OPERANDS_NATIVE 0 /* one pass of the form's type (BF16 / TF32): rounding floor ~1e-3 */
-#define MCB_NS_OPERANDS_SPLIT 1  /* FP32-accurate: each operand split into three BF16 pieces (default) */
-#define MCB_NS_OPERANDS_FP32 2   /* FP32 FMA, no tensor cores (reference point) */
+#define MCB_NS_OPERANDS_SPLIT 1  /* FP32-accurate: three BF16 pieces per operand, own tcgen05 kernel (default) */
+#define MCB_NS_OPERANDS_FP32 2   /* FP32 FMA through cuBLAS, no tensor cores (reference point) */
+#define MCB_NS_OPERANDS_CUBLAS_SPLIT 3 /* cuBLAS's BF16x9 emulation of FP32 (reference point) */
 #define MCB_FLAG_LEARNED 0x200 /* learned cut ranking + dual warm start (models set by mcb_set_models) */
 #define MCB_FLAG_LOG 0x400     /* log the learned models' training pairs (mcb_log_fetch) */
 
@@ -181,6 +182,14 @@ int mcb_project_psd(int n, const double *W, int proj, double *Xp, double *Q, dou
 #define MCB_NOALLOC_MAX_N 512
 int mcb_project_psd_noalloc(int n, const double *W, double *Xp, double *Q, double *Z, double *evals, int *M,
                             void *stream);
+/* The tensor-core GEMM of the Newton-Schulz form (no counterpart in the
+ * reference): C = alpha A B^T + diag I for `batch` row-major npad x npad FP32
+ * matrices (host buffers), each operand split into three BF16 pieces, six piece
+ * products accumulated in FP32 by tcgen05.mma.  npad a multiple of 128, <= 1024.
+ * sym = 1 computes the lower 128 x 128 tiles only and mirrors them (for products
+ * known to be symmetric). */
+int mcb_split_gemm(int npad, int batch, const float *A, const float *B, float alpha, float diag, int sym,
+                   float *C);
 /* largest eigenvalue (admm.c:731-752) and a rigorous upper bound on it */
 int mcb_lambda_max(int n, const double *A, double *lmax, double *lmax_upper);
 /* basic SDP relaxation by the predictor-corrector IPM, ipm_mc_pk.c */
@@ -244,7 +253,9 @@ int mcb_kernel_work(const mcb_ctx *ctx, int cap, double *work, int *unit);
 void mcb_transfer_stats(const mcb_ctx *ctx, long long *h2d_bytes, long long *d2h_bytes);
 /* FP64 FMA throughput of the current device in GFLOP/s (microbenchmark) */
 double mcb_measure_fp64_peak(void);
+/* launches of the library's own kernels, and of cuBLAS GEMMs (Newton-Schulz forms) */
 long long mcb_launch_count(const mcb_ctx *ctx);
+long long mcb_library_launch_count(const mcb_ctx *ctx);
 
 #ifdef __cplusplus
 }

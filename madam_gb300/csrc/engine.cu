@@ -149,7 +149,8 @@ struct mcb_ctx {
     float *d_F = nullptr, *d_pred = nullptr;
     size_t fcap = 0;
     // instrumentation
-    long long h2d = 0, d2h = 0;        // host<->device bytes moved by the bound calls
+    long long h2d = 0, d2h = 0;
+    long long lib_launches = 0;        // cuBLAS launches (not counted as own kernels)        // host<->device bytes moved by the bound calls
     double work[K_NCLASS] = {};        // algorithmic work per class (flops or bytes, see kWorkUnit)
     long long launches[K_NCLASS] = {};
     double ms[K_NCLASS] = {};
@@ -378,15 +379,27 @@ void launch_projection(mcb_ctx *c, int ns, int gate) {
 int launch_ns_projection(mcb_ctx *c, int ns) {
     Slot *d = c->d_slots;
     NsProj &P = c->ns;
-    { Prof p(c, K_NSPREP, 2); launch_ns_prep(d, ns, P.npad, P.stride, P.S, P.Wd, 1, c->st); }
+    {
+        Prof p(c, K_NSPREP, P.tc() ? 4 : 2);
+        launch_ns_prep(d, ns, P.npad, P.stride, P.S, P.Wd, 1, c->st);
+        if (P.tc()) P.split_inputs(c->st);
+    }
     double lo = P.flops_lo, hi = P.flops_hi, f64 = P.flops_fp64;
     int rc;
     {
-        Prof p(c, K_NSGEMM, 3 * (int)P.steps.size() + 1);
+        // tcgen05 path: two own GEMM kernels per step and the closing trace; cuBLAS
+        // paths: one diagonal update per step and the closing conversion, the GEMMs
+        // are cuBLAS launches, counted apart
+        Prof p(c, K_NSGEMM, (P.tc() ? 2 : 1) * (int)P.steps.size() + 1);
         rc = P.sign(d, ns, 1, c->st);
+        if (!P.tc()) c->lib_launches += 2 * (long long)P.steps.size();
     }
     if (rc) return set_err(c, rc, "cuBLAS GEMM of the Newton-Schulz step failed");
-    { Prof p(c, K_NSREF, 1); rc = P.product(c->st); }
+    {
+        Prof p(c, K_NSREF, P.tc() ? 1 : 0);
+        rc = P.product(c->st);
+        if (!P.tc()) c->lib_launches += 1;
+    }
     if (rc) return set_err(c, rc, "cuBLAS FP64 GEMM of the projection failed");
     c->work[K_NSGEMM] += (P.flops_lo - lo) + (P.flops_hi - hi);
     c->work[K_NSREF] += P.flops_fp64 - f64;
@@ -872,7 +885,8 @@ int ns_hyperplanes(mcb_ctx *c, std::vector<NodeRun *> &runs, std::vector<NodeRun
     CUDA_TRY(c, h2d(c, c->d_hkeys, keys.data(), k * sizeof(unsigned long long)));
     int rc;
     {
-        Prof p(c, K_HEUR, 4);
+        Prof p(c, K_HEUR, 3);
+        c->lib_launches += 1;
         rc = c->ns.hyperplanes(c->d_slots, list, c->d_hlist, c->d_hkeys, count, (nm + 15) / 16 * 16, c->d_hsign,
                                ostride, c->st);
     }
@@ -1084,16 +1098,23 @@ int bound_batch(mcb_ctx *c, mcb_bab_node *const *nodes, int count, int rank, dou
             std::vector<int> nb0(ns);
             for (int si = 0; si < ns; ++si) nb0[si] = c->hs[si].nbit;
             if (c->proj != MCB_PROJ_FP64) {
-                std::vector<int> lv;
+                std::vector<int> lv, ln;
                 int nm = 1;
                 for (int si = 0; si < ns; ++si)
-                    if (live[si] && !c->hs[si].stop) { lv.push_back(si); nm = std::max(nm, c->hs[si].n); }
-                if ((rc = c->ns.set_live(lv, (nm + 15) / 16 * 16, c->st))) return set_err(c, rc, "pointer upload");
+                    if (live[si] && !c->hs[si].stop) {
+                        lv.push_back(si);
+                        ln.push_back(c->hs[si].n);
+                        nm = std::max(nm, c->hs[si].n);
+                    }
+                if ((rc = c->ns.set_live(lv, ln, c->ns.pad(nm), c->st)))
+                    return set_err(c, rc, "live-slot upload or TMA descriptors");
             }
             for (int k = 0; k < chunk; ++k)
                 if ((rc = launch_admm_iteration(c, ns, mmax, emax))) return rc;
             it += chunk;
             if ((rc = download_slots(c, ns))) return rc;
+            if (c->proj != MCB_PROJ_FP64 && (rc = c->ns.check_error(c->st)))
+                return set_err(c, rc, "a tensor-core wait expired");
             for (int si = 0; si < ns; ++si) {
                 if (!live[si]) continue;
                 const Slot &s2 = c->hs[si];
@@ -1598,7 +1619,9 @@ int mcb_kernel_stats(const mcb_ctx *c, int cap, char (*names)[32], long long *la
 void mcb_reset_kernel_stats(mcb_ctx *c) {
     for (int i = 0; i < K_NCLASS; ++i) { c->launches[i] = 0; c->ms[i] = 0; c->work[i] = 0; }
     c->h2d = c->d2h = 0;
+    c->lib_launches = 0;
 }
+long long mcb_library_launch_count(const mcb_ctx *c) { return c ? c->lib_launches : 0; }
 void mcb_transfer_stats(const mcb_ctx *c, long long *h2d_bytes, long long *d2h_bytes) {
     if (h2d_bytes) *h2d_bytes = c->h2d;
     if (d2h_bytes) *d2h_bytes = c->d2h;

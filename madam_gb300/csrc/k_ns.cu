@@ -11,6 +11,7 @@
 #include "../../include/mcbound.h"
 #include "mcb_dev.cuh"
 #include "ns.h"
+#include "tc.h"
 
 namespace mcb {
 
@@ -84,10 +85,11 @@ __global__ void __launch_bounds__(256) k_ns_finish(Slot *slots, int npad, size_t
     Slot &s = slots[blockIdx.y];
     if (!gated(s, gate)) return;
     const float *Sb = S + (size_t)blockIdx.y * stride;
-    double *Db = Sd + (size_t)blockIdx.y * stride;
+    double *Db = Sd ? Sd + (size_t)blockIdx.y * stride : nullptr;
     const size_t tot = (size_t)npad * npad;
-    for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < tot; q += (size_t)gridDim.x * blockDim.x)
-        Db[q] = (double)Sb[q];
+    if (Sd)
+        for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < tot; q += (size_t)gridDim.x * blockDim.x)
+            Db[q] = (double)Sb[q];
     if (blockIdx.x == 0) {
         __shared__ double red[40];
         double t = 0.0;
@@ -219,7 +221,7 @@ int NsProj::init(int form_, int nmax_, int cap_, cudaStream_t st) {
     form = form_;
     nmax = nmax_;
     cap = cap_;
-    int np = (nmax + 15) / 16 * 16;
+    int np = (nmax + 127) / 128 * 128;
     stride = (size_t)np * np;
     if (cublasCreate(&h) != CUBLAS_STATUS_SUCCESS) return MCB_ERR_CUDA;
     cublasSetStream(h, st);
@@ -232,12 +234,20 @@ int NsProj::init(int form_, int nmax_, int cap_, cudaStream_t st) {
     if (cudaMalloc(&Gd, tot * sizeof(double)) != cudaSuccess) return MCB_ERR_NOMEM;
     if (cudaMalloc(&dptr, 6 * (size_t)cap * sizeof(void *)) != cudaSuccess) return MCB_ERR_NOMEM;
     hptr.assign(6 * (size_t)cap, nullptr);
+    for (__nv_bfloat16 **b : {&Sp, &S2p, &Tp, &Wp})
+        if (cudaMalloc(b, 3 * tot * sizeof(__nv_bfloat16)) != cudaSuccess) return MCB_ERR_NOMEM;
+    if (cudaMalloc(&d_live, cap * sizeof(int)) != cudaSuccess) return MCB_ERR_NOMEM;
+    if (cudaMalloc(&d_n, cap * sizeof(int)) != cudaSuccess) return MCB_ERR_NOMEM;
+    if (cudaMalloc(&d_err, sizeof(int)) != cudaSuccess) return MCB_ERR_NOMEM;
+    cudaMemset(d_err, 0, sizeof(int));
+    maps_store.assign(12 * 128 + 64, 0);
+    maps = (unsigned char *)(((uintptr_t)maps_store.data() + 63) & ~(uintptr_t)63);
     steps = ns_schedule(l0, 0.02, 1e-7);
     return MCB_OK;
 }
 
 int NsProj::configure(int operands_, double l0_) {
-    if (operands_ < MCB_NS_OPERANDS_NATIVE || operands_ > MCB_NS_OPERANDS_FP32 || !(l0_ > 0.0 && l0_ < 0.5))
+    if (operands_ < MCB_NS_OPERANDS_NATIVE || operands_ > MCB_NS_OPERANDS_CUBLAS_SPLIT || !(l0_ > 0.0 && l0_ < 0.5))
         return MCB_ERR_ARG;
     operands = operands_;
     l0 = l0_;
@@ -246,19 +256,41 @@ int NsProj::configure(int operands_, double l0_) {
 }
 
 void NsProj::destroy() {
-    void *ps[] = {S, S2, T, Wd, Sd, Gd, dptr};
+    void *ps[] = {S, S2, T, Wd, Sd, Gd, dptr, Sp, S2p, Tp, Wp, d_live, d_n, d_err};
     for (void *p : ps)
         if (p) cudaFree(p);
     S = S2 = T = nullptr;
+    Sp = S2p = Tp = Wp = nullptr;
+    d_live = d_n = d_err = nullptr;
     Wd = Sd = Gd = nullptr;
     dptr = nullptr;
     if (h) cublasDestroy(h);
     h = nullptr;
 }
 
-int NsProj::set_live(const std::vector<int> &slots, int npad_, cudaStream_t st) {
+int NsProj::set_live(const std::vector<int> &slots, const std::vector<int> &ns, int npad_, cudaStream_t st) {
     live = (int)slots.size();
     npad = npad_;
+    if (tc()) {
+        if (npad % kTcTile) return MCB_ERR_ARG;
+        if (live) {
+            if (cudaMemcpyAsync(d_live, slots.data(), live * sizeof(int), cudaMemcpyHostToDevice, st) != cudaSuccess)
+                return MCB_ERR_CUDA;
+            if (cudaMemcpyAsync(d_n, ns.data(), live * sizeof(int), cudaMemcpyHostToDevice, st) != cudaSuccess)
+                return MCB_ERR_CUDA;
+        }
+        if (map_npad != npad) {
+            __nv_bfloat16 *bufs[4] = {Sp, S2p, Tp, Wp};
+            const size_t tot = stride * (size_t)cap;
+            for (int b = 0; b < 4; ++b)
+                for (int p = 0; p < 3; ++p)
+                    if (int rc = tc_make_map(maps + (3 * b + p) * 128, bufs[b] + p * tot, npad, stride, cap))
+                        return rc;
+            map_npad = npad;
+        }
+        if (cudaStreamSynchronize(st) != cudaSuccess) return MCB_ERR_CUDA;
+        return MCB_OK;
+    }
     for (int k = 0; k < live; ++k) {
         size_t o = slot_offset(slots[k]);
         hptr[0 * cap + k] = S + o;
@@ -285,16 +317,55 @@ cublasStatus_t gemm32(cublasHandle_t h, int np, float alpha, void **A, void **B,
 }
 }  // namespace
 
+int NsProj::check_error(cudaStream_t st) {
+    if (!d_err) return MCB_OK;
+    int e = 0;
+    if (cudaMemcpyAsync(&e, d_err, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess) return MCB_ERR_CUDA;
+    if (cudaStreamSynchronize(st) != cudaSuccess) return MCB_ERR_CUDA;
+    if (e) cudaMemsetAsync(d_err, 0, sizeof(int), st);
+    return e ? MCB_ERR_ITER : MCB_OK;
+}
+
+void NsProj::split_inputs(cudaStream_t st) {
+    const size_t tot = stride * (size_t)cap;
+    TcOut os{nullptr, nullptr, {Sp, Sp + tot, Sp + 2 * tot}, stride, nullptr};
+    TcOut ow{nullptr, nullptr, {Wp, Wp + tot, Wp + 2 * tot}, stride, nullptr};
+    tc_split_f32(S, stride, os, npad, live, d_live, st);
+    tc_split_f64(Wd, stride, ow, npad, live, d_live, st);
+}
+
 int NsProj::sign(Slot *d_slots, int ns, int gate, cudaStream_t st) {
     if (live == 0) return MCB_OK;
+    if (tc()) {
+        const size_t tot = stride * (size_t)cap;
+        __nv_bfloat16 *bufs[3] = {Sp, S2p, Tp};
+        int c = 0, nx = 1;
+        const double g = 2.0 * (double)npad * npad * npad * live;
+        for (size_t i = 0; i < steps.size(); ++i) {
+            const NsStep &stp = steps[i];
+            // T = b S^2 + a I (pieces), then S' = S T (pieces; FP32 after the last step)
+            TcOut ot{nullptr, nullptr, {Tp, Tp + tot, Tp + 2 * tot}, stride, d_err};
+            if (int rc = tc_gemm(maps + 3 * c * 128, maps + 3 * c * 128, ot, npad, live, d_live, d_n, stp.b, stp.a, st, 1))
+                return rc;
+            __nv_bfloat16 *o = bufs[nx];
+            TcOut os{i + 1 == steps.size() ? S : nullptr, nullptr, {o, o + tot, o + 2 * tot}, stride, d_err};
+            if (int rc = tc_gemm(maps + 3 * c * 128, maps + 3 * 2 * 128, os, npad, live, d_live, d_n, 1.0f, 0.0f, st, 1))
+                return rc;
+            flops_hi += 2.0 * g;  // algorithmic: two n^3 products per step (the mirror halves the MMAs)
+            std::swap(c, nx);
+        }
+        cur = c;
+        launch_ns_finish(d_slots, ns, npad, stride, S, nullptr, gate, st);
+        return MCB_OK;
+    }
     cublasSetStream(h, st);
     void **pS = dptr, **pS2 = dptr + cap, **pT = dptr + 2 * cap;
-    // growth steps: one pass of the form's type (NATIVE), its FP32-accurate split
-    // (SPLIT: three BF16 pieces per operand, nine products), or FP32 FMA (FP32);
-    // the closing steps always FP32-accurate
+    // cuBLAS forms: growth steps in one pass of the form's type (NATIVE), its
+    // FP32-accurate split (CUBLAS_SPLIT: cuBLAS's three-piece BF16 emulation), or
+    // FP32 FMA (FP32); the closing steps always FP32-accurate
     const cublasComputeType_t split = CUBLAS_COMPUTE_32F_EMULATED_16BFX9;
     cublasComputeType_t lo = form == MCB_PROJ_NS_TF32 ? CUBLAS_COMPUTE_32F_FAST_TF32 : CUBLAS_COMPUTE_32F_FAST_16BF;
-    if (operands == MCB_NS_OPERANDS_SPLIT) lo = split;
+    if (operands == MCB_NS_OPERANDS_CUBLAS_SPLIT) lo = split;
     if (operands == MCB_NS_OPERANDS_FP32) lo = CUBLAS_COMPUTE_32F;
     const cublasComputeType_t hi = operands == MCB_NS_OPERANDS_FP32 ? CUBLAS_COMPUTE_32F : split;
     float *cur = S, *nxt = S2;
@@ -316,6 +387,12 @@ int NsProj::sign(Slot *d_slots, int ns, int gate, cudaStream_t st) {
 
 int NsProj::product(cudaStream_t st) {
     if (live == 0) return MCB_OK;
+    if (tc()) {
+        TcOut og{nullptr, Gd, {nullptr, nullptr, nullptr}, stride, d_err};
+        int rc = tc_gemm(maps + 3 * 3 * 128, maps + 3 * cur * 128, og, npad, live, d_live, d_n, 1.0f, 0.0f, st, 1);
+        flops_hi += 2.0 * (double)npad * npad * npad * live;
+        return rc;
+    }
     cublasSetStream(h, st);
     void **pW = dptr + 3 * cap, **pSd = dptr + 4 * cap, **pG = dptr + 5 * cap;
     const double one = 1.0, zero = 0.0;

@@ -19,9 +19,12 @@
 // X+ = (W + (WS + SW)/2) / 2 and Q = X+ - W in FP64.
 #pragma once
 #include <cublas_v2.h>
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <vector>
+
+#include "../../include/mcbound.h"
 
 namespace mcb {
 struct Slot;
@@ -38,6 +41,15 @@ std::vector<NsStep> ns_schedule(double l0, double safety, double eps);
 struct NsProj {
     int form = 0;        // MCB_PROJ_NS_BF16 or MCB_PROJ_NS_TF32
     int operands = 1;    // MCB_NS_OPERANDS_* of the growth steps
+    // SPLIT operands run on the library's own tcgen05 kernel (k_tc.cu): every
+    // matrix as three BF16 pieces, npad a multiple of 128, G = W S from pieces
+    bool tc() const { return operands == MCB_NS_OPERANDS_SPLIT; }
+    __nv_bfloat16 *Sp = nullptr, *S2p = nullptr, *Tp = nullptr, *Wp = nullptr;  // 3 * cap * stride each
+    int *d_live = nullptr, *d_n = nullptr, *d_err = nullptr;
+    unsigned char *maps = nullptr;  // 12 TMA descriptors: S, S2, T, W pieces (64-byte aligned)
+    std::vector<unsigned char> maps_store;
+    int map_npad = 0;
+    int cur = 0;                    // which of S / S2 holds the result of sign()
     int nmax = 0;        // largest matrix order
     int cap = 0;         // slots
     size_t stride = 0;   // elements per slot region (npad_max^2)
@@ -58,7 +70,7 @@ struct NsProj {
     int configure(int operands_, double l0_);
     void destroy();
     // set the live slots (indices into the slot array) and the padded order
-    int set_live(const std::vector<int> &slots, int npad_, cudaStream_t st);
+    int set_live(const std::vector<int> &slots, const std::vector<int> &ns, int npad_, cudaStream_t st);
     // sign(W) for the live slots from the scaled W of launch_ns_prep (gate = 1
     // skips slots whose ADMM has stopped), into Sd in FP64, and M per slot
     int sign(Slot *d_slots, int ns, int gate, cudaStream_t st);
@@ -70,6 +82,12 @@ struct NsProj {
                     const unsigned long long *d_keys, int count, int npad_, unsigned char *d_out, size_t out_stride,
                     cudaStream_t st);
     size_t slot_offset(int slot) const { return (size_t)slot * stride; }
+    // order of the padded matrices for the live slots' largest n
+    int pad(int nmax_live) const { return tc() ? (nmax_live + 127) / 128 * 128 : (nmax_live + 15) / 16 * 16; }
+    // three BF16 pieces of the scaled W (S) and of W for the live slots (tcgen05 path)
+    void split_inputs(cudaStream_t st);
+    // MCB_ERR_ITER when a bounded wait of a tcgen05 kernel expired (flag reset)
+    int check_error(cudaStream_t st);
 };
 
 // kernels (k_ns.cu)

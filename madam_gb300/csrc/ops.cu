@@ -10,6 +10,7 @@
 #include "kernels.h"
 #include "mcb_dev.cuh"
 #include "ns.h"
+#include "tc.h"
 
 using namespace mcb;
 
@@ -119,13 +120,15 @@ int project_ns(OneSlot &S, int n, int proj) {
     int rc = P.init(proj & 0xf, n, 1, 0);
     if (rc == MCB_OK && (proj >> 4)) rc = P.configure(((proj >> 4) & 0xf) - 1, P.l0);
     if (rc == MCB_OK) {
-        const int npad = (n + 15) / 16 * 16;
-        rc = P.set_live({0}, npad, 0);
+        const int npad = P.pad(n);
+        rc = P.set_live({0}, {n}, npad, 0);
         if (rc == MCB_OK) launch_ns_prep(S.d, 1, npad, P.stride, P.S, P.Wd, 0, 0);
+        if (rc == MCB_OK && P.tc()) P.split_inputs(0);
         if (rc == MCB_OK) rc = P.sign(S.d, 1, 0, 0);
         if (rc == MCB_OK) rc = P.product(0);
         if (rc == MCB_OK) launch_ns_post0(S.d, 1, n, P.Gd, npad, P.stride, 0);
         if (rc == MCB_OK && cudaDeviceSynchronize() != cudaSuccess) rc = MCB_ERR_CUDA;
+        if (rc == MCB_OK) rc = P.check_error(0);
     }
     P.destroy();
     return rc;
@@ -323,6 +326,54 @@ int mcb_qap_sa_batch(int n, const double *X, int k, int trials, uint64_t key, in
     for (int r = 0; r < runs; ++r)
         for (int a = 0; a < k; ++a) ineq[(size_t)r * k + a] = o[(size_t)r * 8 + a];
     return cuda_rc(cudaDeviceSynchronize());
+}
+
+int mcb_split_gemm(int npad, int batch, const float *A, const float *B, float alpha, float diag, int sym, float *C) {
+    if (npad < kTcTile || npad % kTcTile || npad > 1024 || batch < 1 || batch > 4096 || !A || !B || !C)
+        return MCB_ERR_ARG;
+    if (int rc = check_dev()) return rc;
+    const size_t nn = (size_t)npad * npad, tot = nn * batch;
+    std::vector<void *> al;
+    cudaError_t e = cudaSuccess;
+    auto mk = [&](size_t bytes) -> void * {
+        void *p = nullptr;
+        if (e == cudaSuccess) e = cudaMalloc(&p, bytes);
+        if (p) al.push_back(p);
+        return p;
+    };
+    float *dA = (float *)mk(tot * 4), *dB = (float *)mk(tot * 4), *dC = (float *)mk(tot * 4);
+    __nv_bfloat16 *pa = (__nv_bfloat16 *)mk(3 * tot * 2), *pb = (__nv_bfloat16 *)mk(3 * tot * 2);
+    int *live = (int *)mk(batch * sizeof(int)), *nl = (int *)mk(batch * sizeof(int)), *err = (int *)mk(sizeof(int));
+    void *maps = mk(6 * tc_map_bytes() + 64);
+    int rc = e == cudaSuccess ? MCB_OK : MCB_ERR_NOMEM;
+    if (rc == MCB_OK) {
+        std::vector<int> l(batch), nv(batch, npad);
+        for (int k = 0; k < batch; ++k) l[k] = k;
+        cudaMemcpy(dA, A, tot * 4, cudaMemcpyHostToDevice);
+        cudaMemcpy(dB, B, tot * 4, cudaMemcpyHostToDevice);
+        cudaMemcpy(live, l.data(), batch * sizeof(int), cudaMemcpyHostToDevice);
+        cudaMemcpy(nl, nv.data(), batch * sizeof(int), cudaMemcpyHostToDevice);
+        cudaMemset(err, 0, sizeof(int));
+        TcOut oa{nullptr, nullptr, {pa, pa + tot, pa + 2 * tot}, nn, nullptr};
+        TcOut ob{nullptr, nullptr, {pb, pb + tot, pb + 2 * tot}, nn, nullptr};
+        tc_split_f32(dA, nn, oa, npad, batch, live, 0);
+        tc_split_f32(dB, nn, ob, npad, batch, live, 0);
+        // host-side maps (64-byte aligned), passed by value to the kernel
+        alignas(64) unsigned char hm[6][128];
+        for (int p = 0; p < 3 && rc == MCB_OK; ++p) {
+            rc = tc_make_map(hm[p], oa.p[p], npad, nn, batch);
+            if (rc == MCB_OK) rc = tc_make_map(hm[3 + p], ob.p[p], npad, nn, batch);
+        }
+        TcOut oc{dC, nullptr, {nullptr, nullptr, nullptr}, nn, err};
+        if (rc == MCB_OK) rc = tc_gemm(hm[0], hm[3], oc, npad, batch, live, nl, alpha, diag, 0, sym);
+        if (rc == MCB_OK && cudaDeviceSynchronize() != cudaSuccess) rc = MCB_ERR_CUDA;
+        int herr = 0;
+        if (rc == MCB_OK) cudaMemcpy(&herr, err, sizeof(int), cudaMemcpyDeviceToHost);
+        if (rc == MCB_OK && herr) rc = herr;
+        if (rc == MCB_OK) cudaMemcpy(C, dC, tot * 4, cudaMemcpyDeviceToHost);
+    }
+    for (void *p : al) cudaFree(p);
+    return rc;
 }
 
 }  // extern "C"

@@ -17,7 +17,7 @@ NMAX = 1024
 
 OK, ERR_ARG, ERR_CUDA, ERR_NOMEM, ERR_NUMERIC, ERR_CAPACITY, ERR_ITER, ERR_NODEV = 0, -1, -2, -3, -4, -5, -6, -7
 PROJ_FP64, PROJ_NS_BF16, PROJ_NS_TF32 = 0x0, 0x1, 0x2
-NS_OPERANDS_NATIVE, NS_OPERANDS_SPLIT, NS_OPERANDS_FP32 = 0, 1, 2
+NS_OPERANDS_NATIVE, NS_OPERANDS_SPLIT, NS_OPERANDS_FP32, NS_OPERANDS_CUBLAS_SPLIT = 0, 1, 2, 3
 
 
 def PROJ_OPERANDS(op):
@@ -145,6 +145,10 @@ def lib():
     L.mcb_log_count.argtypes = [C.c_void_p, C.c_int]
     L.mcb_log_fetch.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p]
     L.mcb_log_clear.argtypes = [C.c_void_p]
+    L.mcb_library_launch_count.restype = C.c_longlong
+    L.mcb_library_launch_count.argtypes = [C.c_void_p]
+    L.mcb_split_gemm.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_float, C.c_float, C.c_int,
+                                 C.c_void_p]
     L.mcb_launch_count.restype = C.c_longlong
     L.mcb_launch_count.argtypes = [C.c_void_p]
     _lib = L
@@ -286,6 +290,9 @@ class Context:
     def launch_count(self):
         return lib().mcb_launch_count(self.h)
 
+    def library_launch_count(self):
+        return lib().mcb_library_launch_count(self.h)
+
 
 class MLP:
     """The learned models' network, trained and evaluated by the library's own kernels."""
@@ -395,6 +402,19 @@ def project_noalloc(n, W_dev, Xp_dev, Q_dev, Z_dev, evals_dev, stream=None):
                                          C.c_void_p(Z_dev), C.c_void_p(evals_dev), C.byref(M),
                                          None if stream is None else C.c_void_p(stream)))
     return M.value
+
+
+def split_gemm(A, B, alpha=1.0, diag=0.0, sym=False):
+    """alpha A[k] B[k]^T + diag I for a batch of square FP32 matrices (tcgen05, split BF16 operands);
+    sym: the product is known to be symmetric (lower tiles computed and mirrored)."""
+    A = np.ascontiguousarray(A, dtype=np.float32)
+    B = np.ascontiguousarray(B, dtype=np.float32)
+    if A.ndim == 2:
+        A, B = A[None], B[None]
+    C = np.zeros_like(A)
+    _check(lib().mcb_split_gemm(A.shape[1], A.shape[0], A.ctypes.data, B.ctypes.data, alpha, diag, int(sym),
+                                C.ctypes.data))
+    return C
 
 
 def lambda_max(A):

@@ -140,3 +140,33 @@ def test_ns_branch_and_bound_reaches_reference_optimum(gpu_lib, fx):
     # every bound of the tree is a valid bound on the cut of its subtree; the root's on the optimum
     assert r["root_bound"] >= fx["opt"]
     ctx.close()
+
+
+@pytest.mark.parametrize("npad,batch", [(128, 1), (256, 3), (512, 2)])
+def test_tcgen05_split_gemm_against_float64(gpu_lib, npad, batch):
+    """The tensor-core GEMM with three-piece BF16 operands is FP32-accurate on
+    general (non-symmetric) matrices: C = alpha A B^T + diag I."""
+    rng = np.random.default_rng(npad + batch)
+    A = rng.standard_normal((batch, npad, npad)).astype(np.float32)
+    B = rng.standard_normal((batch, npad, npad)).astype(np.float32)
+    C = gpu_lib.split_gemm(A, B, alpha=-0.75, diag=1.5)
+    ref = -0.75 * np.einsum("bik,bjk->bij", A.astype(np.float64), B.astype(np.float64)) + 1.5 * np.eye(npad)
+    assert np.abs(C - ref).max() <= 1e-5 * np.abs(ref).max()
+
+
+def test_tcgen05_split_gemm_rejects_bad_sizes(gpu_lib):
+    with pytest.raises(gpu_lib.MCBError):
+        gpu_lib.split_gemm(np.zeros((1, 100, 100)), np.zeros((1, 100, 100)))
+
+
+@pytest.mark.parametrize("npad", [128, 384])
+def test_tcgen05_symmetric_product_is_exactly_symmetric(gpu_lib, npad):
+    """sym = 1: lower tiles computed and mirrored; the result is bit-symmetric and
+    FP32-accurate for a product known to be symmetric (A A^T)."""
+    rng = np.random.default_rng(npad)
+    A = rng.standard_normal((2, npad, npad)).astype(np.float32)
+    A = A + A.transpose(0, 2, 1)
+    C = gpu_lib.split_gemm(A, A, alpha=0.5, diag=-1.0, sym=True)
+    ref = 0.5 * np.einsum("bik,bjk->bij", A.astype(np.float64), A.astype(np.float64)) - np.eye(npad)
+    assert np.array_equal(C, C.transpose(0, 2, 1))
+    assert np.abs(C - ref).max() <= 1e-5 * np.abs(ref).max()
