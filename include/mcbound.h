@@ -187,9 +187,18 @@ int mcb_project_psd_noalloc(int n, const double *W, double *Xp, double *Q, doubl
  * matrices (host buffers), each operand split into three BF16 pieces, six piece
  * products accumulated in FP32 by tcgen05.mma.  npad a multiple of 128, <= 1024.
  * sym = 1 computes the lower 128 x 128 tiles only and mirrors them (for products
- * known to be symmetric). */
+ * known to be symmetric).  variant: 0 = one pipeline stage, two CTAs per SM;
+ * 1 = two stages, one CTA per SM (the autotuner picks per matrix order). */
 int mcb_split_gemm(int npad, int batch, const float *A, const float *B, float alpha, float diag, int sym,
-                   float *C);
+                   int variant, float *C);
+/* The autotuner's table of a context (Newton-Schulz forms): for every (npad,
+ * live-slot bucket) met so far the chosen tcgen05 variant and the microseconds
+ * per launch each variant took.  Returns the number of entries. */
+int mcb_autotune_table(const mcb_ctx *ctx, int cap, int *npad, int *bucket, int *variant, float *us0, float *us1);
+/* Save / load the table as JSON ({"tc_gemm": [{"npad":..,"bucket":..,"variant":..,"us":[..,..]}]});
+ * loaded entries are used instead of timing. */
+int mcb_autotune_save(const mcb_ctx *ctx, const char *path);
+int mcb_autotune_load(mcb_ctx *ctx, const char *path);
 /* largest eigenvalue (admm.c:731-752) and a rigorous upper bound on it */
 int mcb_lambda_max(int n, const double *A, double *lmax, double *lmax_upper);
 /* basic SDP relaxation by the predictor-corrector IPM, ipm_mc_pk.c */
@@ -256,6 +265,10 @@ double mcb_measure_fp64_peak(void);
 /* launches of the library's own kernels, and of cuBLAS GEMMs (Newton-Schulz forms) */
 long long mcb_launch_count(const mcb_ctx *ctx);
 long long mcb_library_launch_count(const mcb_ctx *ctx);
+/* ADMM chunks run as CUDA graphs when profiling is off: graphs captured, and replays */
+void mcb_graph_stats(const mcb_ctx *ctx, long long *captures, long long *replays);
+/* switch per-class CUDA-event timing (MCB_FLAG_PROFILE) on or off between calls */
+void mcb_set_profile(mcb_ctx *ctx, int on);
 
 #ifdef __cplusplus
 }

@@ -61,9 +61,10 @@ __global__ void k_admm_rhs(Slot *slots) {
 }
 
 // (B B^T + I) t = rhs by conjugate gradients, warm-started from the current t,
-// to ||r|| <= 1e-13 ||rhs|| (the reference factors with CHOLMOD, admm.c:546).
-// One CTA per slot.  An iteration cap sets status and leaves t as is.
-__global__ void __launch_bounds__(1024) k_cg(Slot *slots, int maxit) {
+// to ||r|| <= rtol ||rhs|| (the reference factors with CHOLMOD, admm.c:546; the
+// plain form uses rtol = 1e-13).  One CTA per slot.  An iteration cap sets
+// status and leaves t as is.
+__global__ void __launch_bounds__(1024) k_cg(Slot *slots, int maxit, double rtol2) {
     Slot &s = slots[blockIdx.x];
     if (!live(s)) return;
     const int m = s.m;
@@ -85,7 +86,7 @@ __global__ void __launch_bounds__(1024) k_cg(Slot *slots, int maxit) {
     }
     double bb = block_sum(lbb, red);
     double rr = block_sum(lrr, red);
-    const double stop2 = 1e-26 * bb;
+    const double stop2 = rtol2 * bb;
     int it = 0;
     while (rr > stop2 && it < maxit) {
         double lpq = 0.0;
@@ -289,7 +290,9 @@ void launch_admm_rhs(Slot *d, int ns, int nmax, int mmax, cudaStream_t st) {
     dim3 g(cdiv(tot, 256), ns);
     k_admm_rhs<<<g, 256, 0, st>>>(d);
 }
-void launch_cg(Slot *d, int ns, int maxit, cudaStream_t st) { k_cg<<<ns, 1024, 0, st>>>(d, maxit); }
+void launch_cg(Slot *d, int ns, int maxit, double rtol, cudaStream_t st) {
+    k_cg<<<ns, 1024, 0, st>>>(d, maxit, rtol * rtol);
+}
 void launch_admm_su(Slot *d, int ns, int mmax, cudaStream_t st) {
     dim3 g(cdiv(mmax > 1 ? mmax : 1, 256) < 512 ? cdiv(mmax > 1 ? mmax : 1, 256) : 512, ns);
     k_admm_su<<<g, 256, 0, st>>>(d);

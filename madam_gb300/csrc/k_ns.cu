@@ -289,6 +289,11 @@ int NsProj::set_live(const std::vector<int> &slots, const std::vector<int> &ns, 
             map_npad = npad;
         }
         if (cudaStreamSynchronize(st) != cudaSuccess) return MCB_ERR_CUDA;
+        if (live) {
+            auto it = tuned.find({npad, bucket(live)});
+            if (it == tuned.end()) return tune(st);
+            variant = it->second.variant;
+        }
         return MCB_OK;
     }
     for (int k = 0; k < live; ++k) {
@@ -316,6 +321,36 @@ cublasStatus_t gemm32(cublasHandle_t h, int np, float alpha, void **A, void **B,
                                batch, ct, CUBLAS_GEMM_DEFAULT);
 }
 }  // namespace
+
+int NsProj::tune(cudaStream_t st) {
+    const size_t tot = stride * (size_t)cap;
+    TcOut ot{nullptr, nullptr, {Tp, Tp + tot, Tp + 2 * tot}, stride, d_err};
+    Tuned t{0, {0.0f, 0.0f}};
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    int rc = MCB_OK;
+    for (int v = 0; v < kTcVariants && rc == MCB_OK; ++v) {
+        float best = 1e30f;
+        for (int rep = 0; rep < 4 && rc == MCB_OK; ++rep) {  // first launch warms up
+            cudaEventRecord(e0, st);
+            rc = tc_gemm(maps, maps, ot, npad, live, d_live, d_n, 1.0f, 0.0f, st, 1, v);
+            cudaEventRecord(e1, st);
+            if (cudaEventSynchronize(e1) != cudaSuccess) rc = MCB_ERR_CUDA;
+            float ms = 0.0f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (rep > 0) best = ms < best ? ms : best;
+        }
+        t.us[v] = best * 1e3f;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc != MCB_OK) return rc;
+    t.variant = t.us[1] < t.us[0] ? 1 : 0;
+    tuned[{npad, bucket(live)}] = t;
+    variant = t.variant;
+    return check_error(st);
+}
 
 int NsProj::check_error(cudaStream_t st) {
     if (!d_err) return MCB_OK;
@@ -345,11 +380,11 @@ int NsProj::sign(Slot *d_slots, int ns, int gate, cudaStream_t st) {
             const NsStep &stp = steps[i];
             // T = b S^2 + a I (pieces), then S' = S T (pieces; FP32 after the last step)
             TcOut ot{nullptr, nullptr, {Tp, Tp + tot, Tp + 2 * tot}, stride, d_err};
-            if (int rc = tc_gemm(maps + 3 * c * 128, maps + 3 * c * 128, ot, npad, live, d_live, d_n, stp.b, stp.a, st, 1))
+            if (int rc = tc_gemm(maps + 3 * c * 128, maps + 3 * c * 128, ot, npad, live, d_live, d_n, stp.b, stp.a, st, 1, variant))
                 return rc;
             __nv_bfloat16 *o = bufs[nx];
             TcOut os{i + 1 == steps.size() ? S : nullptr, nullptr, {o, o + tot, o + 2 * tot}, stride, d_err};
-            if (int rc = tc_gemm(maps + 3 * c * 128, maps + 3 * 2 * 128, os, npad, live, d_live, d_n, 1.0f, 0.0f, st, 1))
+            if (int rc = tc_gemm(maps + 3 * c * 128, maps + 3 * 2 * 128, os, npad, live, d_live, d_n, 1.0f, 0.0f, st, 1, variant))
                 return rc;
             flops_hi += 2.0 * g;  // algorithmic: two n^3 products per step (the mirror halves the MMAs)
             std::swap(c, nx);
@@ -389,7 +424,8 @@ int NsProj::product(cudaStream_t st) {
     if (live == 0) return MCB_OK;
     if (tc()) {
         TcOut og{nullptr, Gd, {nullptr, nullptr, nullptr}, stride, d_err};
-        int rc = tc_gemm(maps + 3 * 3 * 128, maps + 3 * cur * 128, og, npad, live, d_live, d_n, 1.0f, 0.0f, st, 1);
+        int rc = tc_gemm(maps + 3 * 3 * 128, maps + 3 * cur * 128, og, npad, live, d_live, d_n, 1.0f, 0.0f, st, 1,
+                         variant);
         flops_hi += 2.0 * (double)npad * npad * npad * live;
         return rc;
     }

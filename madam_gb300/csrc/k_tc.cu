@@ -18,9 +18,11 @@
 //
 // Tiling: one CTA per 128 x 128 tile of C and slot; K in chunks of 64 BF16
 // (one 128-byte swizzle row).  A stage holds the three pieces of the A and B
-// chunks (96 KB), two stages double-buffer the TMA loads against the MMAs.  One
-// thread issues the TMA copies and the MMAs; all four warps drain the
-// accumulator (32 lanes each) with tcgen05.ld.  Every wait on an mbarrier is
+// chunks (96 KB); with one stage per CTA two CTAs fit on an SM (shared memory
+// and the 512 tensor-memory columns), so one CTA's TMA loads overlap the other's
+// MMAs and a 64-slot batch of 256 x 256 products runs in one wave.  One thread
+// issues the TMA copies and the MMAs; all four warps drain the accumulators (32
+// lanes each) with tcgen05.ld, through a shared-memory tile for coalesced stores.  Every wait on an mbarrier is
 // bounded: on expiry the CTA records an error code and skips the rest.
 #include <cuda.h>
 #include <cuda_bf16.h>
@@ -40,8 +42,10 @@ constexpr int BM = 128, BN = 128, BK = 64;
 constexpr int kPieces = 3;
 constexpr int kTileBytes = BM * BK * 2;                   // one piece of one operand chunk (16 KB)
 constexpr int kStageBytes = 2 * kPieces * kTileBytes;    // A and B, three pieces each (96 KB)
-constexpr int kStages = 2;
-constexpr int kSmemBytes = kStages * kStageBytes + 1024 + 128;
+// two variants, picked per matrix order by the autotuner (tc_variant): one stage
+// per CTA with two CTAs per SM, or two stages (TMA of chunk k+1 under the MMAs of
+// chunk k) with one CTA per SM
+constexpr int smem_bytes(int stages) { return stages * kStageBytes + 1024 + 128; }
 constexpr uint32_t kTmemCols = 256;  // two 128-column FP32 accumulators: hi.hi, and the corrections
 constexpr long long kSpinLimit = 1ll << 26;  // bounded waits (~a second)
 
@@ -130,7 +134,8 @@ struct Maps {
     CUtensorMap a[kPieces], b[kPieces];
 };
 
-__global__ void __launch_bounds__(128, 1) k_tc_gemm(const __grid_constant__ Maps maps, TcOut out, int npad,
+template <int kStages>
+__global__ void __launch_bounds__(128, 3 - kStages) k_tc_gemm(const __grid_constant__ Maps maps, TcOut out, int npad,
                                                    const int *live, const int *nlist, float alpha, float diag,
                                                    int sym) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
@@ -175,7 +180,7 @@ __global__ void __launch_bounds__(128, 1) k_tc_gemm(const __grid_constant__ Maps
     if (tid == 0) {
         const uint32_t idesc = instr_desc(BM, BN);
         auto load = [&](int kc) {
-            const int s = kc & 1;
+            const int s = kc % kStages;
             unsigned char *st = smem + s * kStageBytes;
             mbar_expect_tx(&full[s], kStageBytes);
             for (int p = 0; p < kPieces; ++p) {
@@ -184,16 +189,11 @@ __global__ void __launch_bounds__(128, 1) k_tc_gemm(const __grid_constant__ Maps
             }
         };
         bool ok = true;
-        load(0);
+        for (int kc = 0; kc < kStages && kc < nk; ++kc) load(kc);
         for (int kc = 0; kc < nk && ok; ++kc) {
-            const int s = kc & 1;
-            if (kc + 1 < nk) {
-                // the other stage was read by the MMAs of chunk kc - 1
-                if (kc >= 1) ok = mbar_wait(&empty[(kc + 1) & 1], ((kc - 1) >> 1) & 1);
-                if (!ok) break;
-                load(kc + 1);
-            }
-            ok = mbar_wait(&full[s], (kc >> 1) & 1);
+            const int s = kc % kStages;
+            const uint32_t use = (uint32_t)(kc / kStages) & 1u;
+            ok = mbar_wait(&full[s], use);
             if (!ok) break;
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             const uint32_t base = smem_u32(smem + s * kStageBytes);
@@ -210,6 +210,12 @@ __global__ void __launch_bounds__(128, 1) k_tc_gemm(const __grid_constant__ Maps
                     mma_bf16(tmem + (q == 0 ? 0u : (uint32_t)BN), ad, bd, idesc, acc);
                 }
             mma_commit(&empty[s]);
+            // refill this stage once its MMAs have read it
+            if (kc + kStages < nk) {
+                ok = mbar_wait(&empty[s], use);
+                if (!ok) break;
+                load(kc + kStages);
+            }
         }
         if (!ok) s_fail = 1;
         mma_commit(done);
@@ -327,12 +333,15 @@ int tc_make_map(void *map, const __nv_bfloat16 *base, int npad, size_t stride, i
 size_t tc_map_bytes() { return sizeof(CUtensorMap); }
 
 int tc_gemm(const void *amaps, const void *bmaps, const TcOut &out, int npad, int nlive, const int *d_live,
-            const int *d_n, float alpha, float diag, cudaStream_t st, int sym) {
+            const int *d_n, float alpha, float diag, cudaStream_t st, int sym, int variant) {
     if (nlive <= 0) return MCB_OK;
-    if (npad % BM || npad % BK) return MCB_ERR_ARG;
+    if (npad % BM || npad % BK || variant < 0 || variant >= kTcVariants) return MCB_ERR_ARG;
     static bool attr = false;
     if (!attr) {
-        if (cudaFuncSetAttribute(k_tc_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes) != cudaSuccess)
+        if (cudaFuncSetAttribute(k_tc_gemm<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes(1)) !=
+                cudaSuccess ||
+            cudaFuncSetAttribute(k_tc_gemm<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes(2)) !=
+                cudaSuccess)
             return MCB_ERR_CUDA;
         attr = true;
     }
@@ -341,7 +350,10 @@ int tc_gemm(const void *amaps, const void *bmaps, const TcOut &out, int npad, in
     memcpy(m.b, bmaps, sizeof(m.b));
     const int nt = npad / BM;
     dim3 grid(sym ? nt * (nt + 1) / 2 : nt * nt, nlive);
-    k_tc_gemm<<<grid, 128, kSmemBytes, st>>>(m, out, npad, d_live, d_n, alpha, diag, sym);
+    if (variant == 0)
+        k_tc_gemm<1><<<grid, 128, smem_bytes(1), st>>>(m, out, npad, d_live, d_n, alpha, diag, sym);
+    else
+        k_tc_gemm<2><<<grid, 128, smem_bytes(2), st>>>(m, out, npad, d_live, d_n, alpha, diag, sym);
     return cudaGetLastError() == cudaSuccess ? MCB_OK : MCB_ERR_CUDA;
 }
 

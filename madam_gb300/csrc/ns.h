@@ -22,6 +22,8 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <map>
+#include <utility>
 #include <vector>
 
 #include "../../include/mcbound.h"
@@ -50,6 +52,21 @@ struct NsProj {
     std::vector<unsigned char> maps_store;
     int map_npad = 0;
     int cur = 0;                    // which of S / S2 holds the result of sign()
+    // autotuner: tcgen05 kernel variant per (npad, live-slot bucket), with the
+    // timings (microseconds per launch) that chose it
+    struct Tuned {
+        int variant;
+        float us[2];
+    };
+    std::map<std::pair<int, int>, Tuned> tuned;
+    int variant = 0;                // variant of the current launch configuration
+    static int bucket(int nlive) {
+        int b = 1;
+        while (b < nlive) b <<= 1;
+        return b;
+    }
+    // time both variants on the live set (outside any stream capture) and keep the faster
+    int tune(cudaStream_t st);
     int nmax = 0;        // largest matrix order
     int cap = 0;         // slots
     size_t stride = 0;   // elements per slot region (npad_max^2)

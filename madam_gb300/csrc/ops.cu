@@ -328,8 +328,10 @@ int mcb_qap_sa_batch(int n, const double *X, int k, int trials, uint64_t key, in
     return cuda_rc(cudaDeviceSynchronize());
 }
 
-int mcb_split_gemm(int npad, int batch, const float *A, const float *B, float alpha, float diag, int sym, float *C) {
-    if (npad < kTcTile || npad % kTcTile || npad > 1024 || batch < 1 || batch > 4096 || !A || !B || !C)
+int mcb_split_gemm(int npad, int batch, const float *A, const float *B, float alpha, float diag, int sym, int variant,
+                   float *C) {
+    if (npad < kTcTile || npad % kTcTile || npad > 1024 || batch < 1 || batch > 4096 || !A || !B || !C ||
+        variant < 0 || variant >= kTcVariants)
         return MCB_ERR_ARG;
     if (int rc = check_dev()) return rc;
     const size_t nn = (size_t)npad * npad, tot = nn * batch;
@@ -365,7 +367,7 @@ int mcb_split_gemm(int npad, int batch, const float *A, const float *B, float al
             if (rc == MCB_OK) rc = tc_make_map(hm[3 + p], ob.p[p], npad, nn, batch);
         }
         TcOut oc{dC, nullptr, {nullptr, nullptr, nullptr}, nn, err};
-        if (rc == MCB_OK) rc = tc_gemm(hm[0], hm[3], oc, npad, batch, live, nl, alpha, diag, 0, sym);
+        if (rc == MCB_OK) rc = tc_gemm(hm[0], hm[3], oc, npad, batch, live, nl, alpha, diag, 0, sym, variant);
         if (rc == MCB_OK && cudaDeviceSynchronize() != cudaSuccess) rc = MCB_ERR_CUDA;
         int herr = 0;
         if (rc == MCB_OK) cudaMemcpy(&herr, err, sizeof(int), cudaMemcpyDeviceToHost);

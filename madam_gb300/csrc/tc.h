@@ -23,8 +23,10 @@ size_t tc_map_bytes();
 int tc_make_map(void *map, const __nv_bfloat16 *base, int npad, size_t stride, int slots);
 // C = alpha A B^T + diag I_n (n = d_n[k] for live slot d_live[k]); amaps / bmaps: three maps each.
 // sym = 1: the product is symmetric; the lower tiles are computed and mirrored
+// variant: 0 = one stage, two CTAs per SM; 1 = two stages, one CTA per SM
+constexpr int kTcVariants = 2;
 int tc_gemm(const void *amaps, const void *bmaps, const TcOut &out, int npad, int nlive, const int *d_live,
-            const int *d_n, float alpha, float diag, cudaStream_t st, int sym);
+            const int *d_n, float alpha, float diag, cudaStream_t st, int sym, int variant);
 // three BF16 pieces of FP32 / FP64 matrices (row-major, source slots `sstride` apart)
 void tc_split_f32(const float *src, size_t sstride, const TcOut &out, int npad, int nlive, const int *d_live,
                   cudaStream_t st);

@@ -145,10 +145,16 @@ def lib():
     L.mcb_log_count.argtypes = [C.c_void_p, C.c_int]
     L.mcb_log_fetch.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p]
     L.mcb_log_clear.argtypes = [C.c_void_p]
+    L.mcb_graph_stats.argtypes = [C.c_void_p, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]
+    L.mcb_set_profile.argtypes = [C.c_void_p, C.c_int]
     L.mcb_library_launch_count.restype = C.c_longlong
     L.mcb_library_launch_count.argtypes = [C.c_void_p]
     L.mcb_split_gemm.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_float, C.c_float, C.c_int,
-                                 C.c_void_p]
+                                 C.c_int, C.c_void_p]
+    L.mcb_autotune_table.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                     C.c_void_p]
+    L.mcb_autotune_save.argtypes = [C.c_void_p, C.c_char_p]
+    L.mcb_autotune_load.argtypes = [C.c_void_p, C.c_char_p]
     L.mcb_launch_count.restype = C.c_longlong
     L.mcb_launch_count.argtypes = [C.c_void_p]
     _lib = L
@@ -284,11 +290,32 @@ class Context:
         k = lib().mcb_ns_schedule(self.h, cap, C.cast(a, C.c_void_p), C.cast(b, C.c_void_p), C.cast(acc, C.c_void_p))
         return [(a[i], b[i], acc[i]) for i in range(min(k, cap))]
 
+    def autotune_table(self):
+        cap = 256
+        a, b, v = (C.c_int * cap)(), (C.c_int * cap)(), (C.c_int * cap)()
+        u0, u1 = (C.c_float * cap)(), (C.c_float * cap)()
+        k = lib().mcb_autotune_table(self.h, cap, *(C.cast(x, C.c_void_p) for x in (a, b, v, u0, u1)))
+        return [dict(npad=a[i], bucket=b[i], variant=v[i], us=(u0[i], u1[i])) for i in range(min(k, cap))]
+
+    def autotune_save(self, path):
+        _check(lib().mcb_autotune_save(self.h, path.encode()), self.h)
+
+    def autotune_load(self, path):
+        _check(lib().mcb_autotune_load(self.h, path.encode()), self.h)
+
     def reset_kernel_stats(self):
         lib().mcb_reset_kernel_stats(self.h)
 
     def launch_count(self):
         return lib().mcb_launch_count(self.h)
+
+    def graph_stats(self):
+        a, b = C.c_longlong(), C.c_longlong()
+        lib().mcb_graph_stats(self.h, C.byref(a), C.byref(b))
+        return a.value, b.value
+
+    def set_profile(self, on):
+        lib().mcb_set_profile(self.h, int(bool(on)))
 
     def library_launch_count(self):
         return lib().mcb_library_launch_count(self.h)
@@ -404,7 +431,7 @@ def project_noalloc(n, W_dev, Xp_dev, Q_dev, Z_dev, evals_dev, stream=None):
     return M.value
 
 
-def split_gemm(A, B, alpha=1.0, diag=0.0, sym=False):
+def split_gemm(A, B, alpha=1.0, diag=0.0, sym=False, variant=0):
     """alpha A[k] B[k]^T + diag I for a batch of square FP32 matrices (tcgen05, split BF16 operands);
     sym: the product is known to be symmetric (lower tiles computed and mirrored)."""
     A = np.ascontiguousarray(A, dtype=np.float32)
@@ -413,7 +440,7 @@ def split_gemm(A, B, alpha=1.0, diag=0.0, sym=False):
         A, B = A[None], B[None]
     C = np.zeros_like(A)
     _check(lib().mcb_split_gemm(A.shape[1], A.shape[0], A.ctypes.data, B.ctypes.data, alpha, diag, int(sym),
-                                C.ctypes.data))
+                                variant, C.ctypes.data))
     return C
 
 

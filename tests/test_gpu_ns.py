@@ -170,3 +170,36 @@ def test_tcgen05_symmetric_product_is_exactly_symmetric(gpu_lib, npad):
     ref = 0.5 * np.einsum("bik,bjk->bij", A.astype(np.float64), A.astype(np.float64)) - np.eye(npad)
     assert np.array_equal(C, C.transpose(0, 2, 1))
     assert np.abs(C - ref).max() <= 1e-5 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("proj", ["fp64", "ns"])
+def test_graph_replay_matches_direct_launches(gpu_lib, proj, tmp_path):
+    """ADMM chunks replayed from CUDA graphs (profiling off) give bit-identical
+    bounds to direct launches (profiling on); the autotuner's table round-trips."""
+    M = gpu_lib
+    n, e, w = G.gnp(70, 0.5, "pm1", seed=8)
+    SL = G.extended_laplacian(n, e, w).ravel(order="F")
+    flags = M.PROJ_FP64 if proj == "fp64" else M.PROJ_NS_BF16
+    fixes = [{}, {3: 1}, {5: 0, 9: 1}, {1: 1, 2: 0}]
+    out = []
+    for prof in (False, True):
+        ctx = M.Context(M.params(include_Hepta=0, use_diff=0), SL, n, batch_max=4,
+                        flags=flags | (M.FLAG_PROFILE if prof else 0))
+        b, st = ctx.bound_batch([M.node(f) for f in fixes])
+        caps, reps = ctx.graph_stats()
+        if prof:
+            assert caps == 0 and reps == 0
+        else:
+            assert caps >= 1 and reps > caps
+        out.append((b, [s.admm_iters for s in st]))
+        if proj == "ns" and not prof:
+            tab = ctx.autotune_table()
+            assert tab and all(t["variant"] in (0, 1) and min(t["us"]) > 0 for t in tab)
+            path = str(tmp_path / "tune.json")
+            ctx.autotune_save(path)
+            ctx2 = M.Context(M.params(include_Hepta=0, use_diff=0), SL, n, batch_max=4, flags=flags)
+            ctx2.autotune_load(path)
+            assert ctx2.autotune_table() == tab
+            ctx2.close()
+        ctx.close()
+    assert np.array_equal(out[0][0], out[1][0]) and out[0][1] == out[1][1]
