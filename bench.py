@@ -269,6 +269,7 @@ def run_ours(a):
     launches = ctx.launch_count()
     lib_launches = ctx.library_launch_count()
     graphs = ctx.graph_stats()
+    host = {k: round(v / a.steps, 4) for k, v in ctx.host_stats().items()}
     h2d, d2h = ctx.transfer_stats()
     tune = ctx.autotune_table() if a.form != "fp64" else []
     # one more step with per-class CUDA events: kernel shares and the roofline's kernel time
@@ -342,6 +343,7 @@ def run_ours(a):
         "gpu_launches": launches,
         "library_launches": lib_launches,
         "graphs": {"captured": graphs[0], "replayed": graphs[1]},
+        "host_phase_seconds_per_step": host,
         "autotune": tune,
         "roofline_step": "kernel shares and roofline from one extra step with per-class CUDA events",
         "roofline": roof,

@@ -265,6 +265,9 @@ double mcb_measure_fp64_peak(void);
 /* launches of the library's own kernels, and of cuBLAS GEMMs (Newton-Schulz forms) */
 long long mcb_launch_count(const mcb_ctx *ctx);
 long long mcb_library_launch_count(const mcb_ctx *ctx);
+/* wall time of the bound calls per phase (ipm, cut_upload, admm, safe_bound,
+ * heuristic, separation, records, other), GPU waits included; returns the count */
+int mcb_host_stats(const mcb_ctx *ctx, int cap, char (*names)[32], double *seconds);
 /* ADMM chunks run as CUDA graphs when profiling is off: graphs captured, and replays */
 void mcb_graph_stats(const mcb_ctx *ctx, long long *captures, long long *replays);
 /* switch per-class CUDA-event timing (MCB_FLAG_PROFILE) on or off between calls */

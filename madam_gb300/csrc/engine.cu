@@ -94,6 +94,7 @@ struct NodeRun : CutLists {
     std::vector<double> Lsub;          // n x n subproblem matrix (host copy for the heuristic)
     std::vector<double> Zf;            // n x M factor of the last projection (times sqrt(sigma))
     std::vector<unsigned char> signs;  // Newton-Schulz form: hyperplane signs (n x N, 1 = negative)
+    bool heur_gpu = false;             // this round's heuristic already ran on the GPU (x, hval set)
     std::vector<int> U;                // subproblem vertex -> original variable (n - 1 entries)
     std::vector<float> pend_F;         // logged cut-scorer features of the last separated triangles
     std::vector<int> pend_pos;         // ... and their positions in tri
@@ -139,6 +140,7 @@ struct mcb_ctx {
     int *d_hlist = nullptr;
     unsigned long long *d_hkeys = nullptr;
     unsigned char *d_hsign = nullptr;
+    double *d_hval = nullptr;
     // learned models (not owned) and the training logs
     mcb_mlp *scorer = nullptr, *warm = nullptr;
     std::vector<float> log_x[2], log_y[2];
@@ -154,6 +156,8 @@ struct mcb_ctx {
     long long g_dl[64] = {};
     double g_dw[64] = {};
     long long graph_launches = 0, graph_captures = 0;
+    // host-side wall time per phase of bound_batch (seconds)
+    double host_s[8] = {};
     // instrumentation
     long long h2d = 0, d2h = 0;
     long long lib_launches = 0;        // cuBLAS launches (not counted as own kernels)        // host<->device bytes moved by the bound calls
@@ -166,6 +170,15 @@ struct mcb_ctx {
 };
 
 namespace {
+
+const char *kHostNames[] = {"ipm", "cut_upload", "admm", "safe_bound", "heuristic", "separation", "records", "other"};
+enum HostPhase { H_IPM, H_CUTS, H_ADMM, H_SAFE, H_HEUR, H_SEP, H_REC, H_OTHER, H_N };
+struct HostTimer {
+    double *acc;
+    std::chrono::steady_clock::time_point t0;
+    explicit HostTimer(double *a) : acc(a), t0(std::chrono::steady_clock::now()) {}
+    ~HostTimer() { *acc += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(); }
+};
 
 // host -> device copy on the context's stream (the source must outlive the copy)
 cudaError_t h2d(mcb_ctx *c, void *dst, const void *src, size_t bytes) {
@@ -335,10 +348,7 @@ bool cuts_valid(const NodeRun &r) {
     return true;
 }
 
-int upload_cuts(mcb_ctx *c, int si, NodeRun &r) {
-    if (!cuts_valid(r)) return set_err(c, MCB_ERR_NUMERIC, "cut list holds an out-of-range vertex index");
-    HostCuts H;
-    build_host_cuts(r, r.n, H);
+int upload_cuts(mcb_ctx *c, int si, NodeRun &r, const HostCuts &H) {
     int m = r.m();
     int rc = ensure_cut_capacity(c, si, m, H.g_ci.size() + 1, H.e_idx.size(), H.e_cut.size());
     if (rc != MCB_OK) return rc;
@@ -578,8 +588,11 @@ void run_heuristic(const mcb_ctx *c, NodeRun &r) {
     r.heur_calls++;
 }
 
-void run_heuristics(mcb_ctx *c, std::vector<NodeRun *> &rs) {
-    if (rs.empty()) return;
+void run_heuristics(mcb_ctx *c, std::vector<NodeRun *> &all) {
+    if (all.empty()) return;
+    std::vector<NodeRun *> rs;
+    for (auto *r : all)
+        if (!r->heur_gpu) rs.push_back(r);
     unsigned hw = std::max(1u, std::thread::hardware_concurrency());
     unsigned nt = std::min<unsigned>(hw, (unsigned)rs.size());
     if (nt <= 1) {
@@ -595,11 +608,13 @@ void run_heuristics(mcb_ctx *c, std::vector<NodeRun *> &rs) {
         for (auto &t : th) t.join();
     }
     // updateSolution in slot order (bab_functions.c:114-134)
-    for (auto *r : rs)
+    for (auto *r : all) {
+        r->heur_gpu = false;
         if (r->hval > c->LB) {
             c->LB = r->hval;
             c->best_sol = r->x;
         }
+    }
 }
 
 // --- learned models: features on the GPU, optional prediction ------------------
@@ -955,10 +970,33 @@ int ns_hyperplanes(mcb_ctx *c, std::vector<NodeRun *> &runs, std::vector<NodeRun
                                ostride, c->st);
     }
     if (rc) return set_err(c, rc, "hyperplane GEMM failed");
+    // the 1-opt of every hyperplane and the cut values, on the GPU; the host keeps
+    // the first best hyperplane (heuristic.c's strict comparison) per node
+    {
+        Prof p(c, K_HEUR, 1);
+        launch_heur_1opt(c->d_slots, c->d_hlist, k, count, c->N, c->d_lists, c->list_stride, c->d_SL, c->d_hsign,
+                         ostride, c->d_hval, c->st);
+    }
+    std::vector<double> hv((size_t)k * count);
+    CUDA_TRY(c, d2h(c, hv.data(), c->d_hval, hv.size() * sizeof(double)));
+    std::vector<unsigned char> best;
     for (int q = 0; q < k; ++q) {
         NodeRun &r = *runs[list[q]];
-        r.signs.resize((size_t)r.n * count);
-        CUDA_TRY(c, d2h(c, r.signs.data(), c->d_hsign + (size_t)q * ostride, r.signs.size()));
+        int bi = 0;
+        for (int h = 1; h < count; ++h)
+            if (hv[(size_t)q * count + h] > hv[(size_t)q * count + bi]) bi = h;
+        best.resize(r.n);
+        CUDA_TRY(c, d2h(c, best.data(), c->d_hsign + (size_t)q * ostride + (size_t)bi * r.n, r.n));
+        r.x.assign(c->pb, 0);
+        int idx = 0;
+        for (int i = 0; i < c->pb; ++i) {
+            if (r.node->xfixed[i]) r.x[i] = r.node->sol[i];
+            else r.x[i] = best[idx++] ? 0 : 1;
+        }
+        r.hval = hv[(size_t)q * count + bi];
+        r.heur_calls++;
+        r.heur_gpu = true;
+        r.signs.clear();
     }
     return MCB_OK;
 }
@@ -1045,6 +1083,13 @@ int make_record(mcb_ctx *c, int si, NodeRun &r, std::shared_ptr<NodeRecord> &out
 // --- the batched SDPbound ----------------------------------------------------
 int bound_batch(mcb_ctx *c, mcb_bab_node *const *nodes, int count, int rank, double *bounds, mcb_node_stats *stats) {
     auto t0 = std::chrono::steady_clock::now();
+    auto t_last = t0;
+    // wall time since the previous tick goes to `phase`
+    auto tick = [&](int phase) {
+        auto t = std::chrono::steady_clock::now();
+        c->host_s[phase] += std::chrono::duration<double>(t - t_last).count();
+        t_last = t;
+    };
     const int N = c->N, pb = c->pb;
     const mcb_params &P = c->prm;
     int rc;
@@ -1115,8 +1160,10 @@ int bound_batch(mcb_ctx *c, mcb_bab_node *const *nodes, int count, int rank, dou
         if ((rc = fetch_lastrow(c, si, R[si].n, row))) return rc;
         store_fracsol(c, R[si], row);
     }
+    tick(H_IPM);
     // first heuristic: empty factor (M = 0), then prune / give-up tests (bounding.c:88-114)
     run_heuristics(c, runs);
+    tick(H_HEUR);
     std::vector<int> want(ns, 0);
     for (int si = 0; si < ns; ++si) {
         NodeRun &r = R[si];
@@ -1132,6 +1179,7 @@ int bound_batch(mcb_ctx *c, mcb_bab_node *const *nodes, int count, int rank, dou
     if ((rc = separate_triangles(c, ns, runs, want))) return rc;
     for (int si = 0; si < ns; ++si)
         if (want[si]) R[si].sep_round++;
+    tick(H_SEP);
     // outer loop (bounding.c:121-236), in lockstep
     std::vector<double> sbuf;
     while (true) {
@@ -1140,6 +1188,26 @@ int bound_batch(mcb_ctx *c, mcb_bab_node *const *nodes, int count, int rank, dou
         for (int si = 0; si < ns; ++si) live[si] = !R[si].done, nlive += live[si];
         if (!nlive) break;
         int mmax = 0, emax = 0;
+        // the per-node sparse structures (B^T incidence, B B^T + I) on host threads
+        std::vector<HostCuts> HC(ns);
+        {
+            std::vector<int> todo;
+            for (int si = 0; si < ns; ++si)
+                if (live[si]) {
+                    if (!cuts_valid(R[si])) return set_err(c, MCB_ERR_NUMERIC, "cut list holds an out-of-range vertex index");
+                    todo.push_back(si);
+                }
+            std::atomic<size_t> next{0};
+            auto work = [&] {
+                size_t q;
+                while ((q = next.fetch_add(1)) < todo.size()) build_host_cuts(R[todo[q]], R[todo[q]].n, HC[todo[q]]);
+            };
+            unsigned nt = std::min<unsigned>(std::max(1u, std::thread::hardware_concurrency()), (unsigned)todo.size());
+            std::vector<std::thread> th;
+            for (unsigned t = 1; t < nt; ++t) th.emplace_back(work);
+            work();
+            for (auto &t : th) t.join();
+        }
         for (int si = 0; si < ns; ++si) {
             Slot &s = c->hs[si];
             s.active = live[si];
@@ -1147,7 +1215,7 @@ int bound_batch(mcb_ctx *c, mcb_bab_node *const *nodes, int count, int rank, dou
             NodeRun &r = R[si];
             r.count++;
             r.oldf = r.f;
-            if ((rc = upload_cuts(c, si, r))) return rc;
+            if ((rc = upload_cuts(c, si, r, HC[si]))) return rc;
             s.sigma = r.sigma;
             s.tol = r.tol;
             s.nbit = 0;
@@ -1156,6 +1224,7 @@ int bound_batch(mcb_ctx *c, mcb_bab_node *const *nodes, int count, int rank, dou
             emax = std::max(emax, s.ne);
         }
         if ((rc = upload_slots(c, ns))) return rc;
+        tick(H_CUTS);
         // ADMM_solver (admm.c:49-771): chunks of iterations until every live slot stopped
         for (int it = 0; it < P.ADMM_itermax + 8;) {
             const int chunk = 8;
@@ -1194,6 +1263,7 @@ int bound_batch(mcb_ctx *c, mcb_bab_node *const *nodes, int count, int rank, dou
                 if (live[si] && !c->hs[si].stop) all = false;
             if (all) break;
         }
+        tick(H_ADMM);
         // safe bound
         {
             Prof p(c, K_SAFE, 6);
@@ -1209,6 +1279,7 @@ int bound_batch(mcb_ctx *c, mcb_bab_node *const *nodes, int count, int rank, dou
             CUDA_TRY(c, d2h(c, &acc[(size_t)si * kAcc], c->hs[si].acc, kAcc * sizeof(double)));
         }
         CUDA_TRY(c, cudaStreamSynchronize(c->st));
+        tick(H_SAFE);
         std::vector<NodeRun *> hrun;
         for (int si = 0; si < ns; ++si) {
             if (!live[si]) continue;
@@ -1240,6 +1311,7 @@ int bound_batch(mcb_ctx *c, mcb_bab_node *const *nodes, int count, int rank, dou
         if (c->proj != MCB_PROJ_FP64 && !hrun.empty())
             if ((rc = ns_hyperplanes(c, runs, hrun))) return rc;
         run_heuristics(c, hrun);
+        tick(H_HEUR);
         std::vector<int> want3(ns, 0), want5(ns, 0), want7(ns, 0), yo5(ns, 0), yo7(ns, 0);
         for (int si = 0; si < ns; ++si) {
             if (!live[si]) continue;
@@ -1284,6 +1356,7 @@ int bound_batch(mcb_ctx *c, mcb_bab_node *const *nodes, int count, int rank, dou
         }
         if (std::any_of(want7.begin(), want7.end(), [](int v) { return v; }))
             if ((rc = separate_kgonal(c, ns, runs, none, want7, yo5, yo7))) return rc;
+        tick(H_SEP);
         for (int si = 0; si < ns; ++si) {
             if (!live[si]) continue;
             NodeRun &r = R[si];
@@ -1306,7 +1379,9 @@ int bound_batch(mcb_ctx *c, mcb_bab_node *const *nodes, int count, int rank, dou
             if ((rc = fetch_lastrow(c, si, r.n, row))) return rc;
             store_fracsol(c, r, row);
         }
+        tick(H_OTHER);
     }
+    tick(H_OTHER);
     const bool want_records = (c->flags & MCB_FLAG_LOG) || ((c->flags & MCB_FLAG_LEARNED) && c->warm);
     c->last_records.assign(ns, nullptr);
     if (want_records)
@@ -1314,6 +1389,7 @@ int bound_batch(mcb_ctx *c, mcb_bab_node *const *nodes, int count, int rank, dou
             if (!R[si].status && !R[si].prune)
                 if ((rc = make_record(c, si, R[si], c->last_records[si]))) return rc;
     flush_prof(c);
+    tick(H_REC);
     int ret = MCB_OK;
     double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     for (int si = 0; si < ns; ++si) {
@@ -1418,6 +1494,7 @@ mcb_ctx *mcb_create(const mcb_params *params, int N, const double *SL, int batch
         if (rc == MCB_OK) chk(cudaMalloc(&c->d_hlist, batch_max * sizeof(int)));
         if (rc == MCB_OK) chk(cudaMalloc(&c->d_hkeys, batch_max * sizeof(unsigned long long)));
         if (rc == MCB_OK) chk(cudaMalloc(&c->d_hsign, (size_t)batch_max * N * N));
+        if (rc == MCB_OK) chk(cudaMalloc(&c->d_hval, (size_t)batch_max * N * sizeof(double)));
     }
     if (rc != MCB_OK) {
         if (status) *status = rc;
@@ -1436,7 +1513,7 @@ void mcb_destroy(mcb_ctx *c) {
     c->ns.destroy();
     void *ps[] = {c->d_SL, c->d_slots, c->d_partials, c->d_lists, c->d_fixed, c->d_trisel, c->d_tout, c->d_toutv,
                   c->d_tbnd, c->d_tbndv, c->d_sajobs, c->d_perm, c->d_saout, c->d_saval,
-                  c->d_hlist, c->d_hkeys, c->d_hsign, c->d_fslot, c->d_fcp, c->d_fextra, c->d_F, c->d_pred};
+                  c->d_hlist, c->d_hkeys, c->d_hsign, c->d_hval, c->d_fslot, c->d_fcp, c->d_fextra, c->d_F, c->d_pred};
     for (void *p : ps)
         if (p) cudaFree(p);
     for (auto &p : c->pending) { cudaEventDestroy(p.second.first); cudaEventDestroy(p.second.second); }
@@ -1738,8 +1815,17 @@ void mcb_reset_kernel_stats(mcb_ctx *c) {
     for (int i = 0; i < K_NCLASS; ++i) { c->launches[i] = 0; c->ms[i] = 0; c->work[i] = 0; }
     c->h2d = c->d2h = 0;
     c->lib_launches = 0;
+    for (double &h : c->host_s) h = 0.0;
 }
 long long mcb_library_launch_count(const mcb_ctx *c) { return c ? c->lib_launches : 0; }
+int mcb_host_stats(const mcb_ctx *c, int cap, char (*names)[32], double *seconds) {
+    int k = 0;
+    for (int i = 0; i < H_N && k < cap; ++i, ++k) {
+        if (names) snprintf(names[k], 32, "%s", kHostNames[i]);
+        if (seconds) seconds[k] = c ? c->host_s[i] : 0.0;
+    }
+    return k;
+}
 void mcb_graph_stats(const mcb_ctx *c, long long *captures, long long *replays) {
     if (captures) *captures = c ? c->graph_captures : 0;
     if (replays) *replays = c ? c->graph_launches : 0;

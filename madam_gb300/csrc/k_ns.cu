@@ -150,6 +150,117 @@ __global__ void __launch_bounds__(256) k_heur_sign(Slot *slots, const int *list,
     }
 }
 
+// One warp per (listed slot, hyperplane): the 1-opt local search of mc_1opt
+// (heuristic.c) from the hyperplane's signs on the subproblem matrix L, then the
+// cut value sol^T SL sol of the full 0/1 solution over the original variables
+// (fixed ones from the node).  L and SL hold quarter-integers, so every FP64 sum
+// here is exact and independent of order.  Lane l owns elements l + 32 j.
+// signs: n bytes per hyperplane (1 = -1), overwritten with the 1-opt result;
+// hval[q * count + h] = the cut value.
+__global__ void __launch_bounds__(128) k_heur_1opt(const Slot *slots, const int *list, int count, int N,
+                                                   const int *lists, int list_stride, const double *SL,
+                                                   unsigned char *signs, size_t sstride, double *hval) {
+    constexpr int PER = kNmax / 32;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int h = blockIdx.x * 4 + warp;
+    const int q = blockIdx.y;
+    __shared__ unsigned words[4][PER];
+    if (h >= count) return;
+    const int si = list[q];
+    const Slot &s = slots[si];
+    const int n = s.n;
+    const double *L = s.L;
+    unsigned char *sg = signs + (size_t)q * sstride + (size_t)h * n;
+    unsigned xneg = 0;
+    for (int j = 0; j < PER; ++j) {
+        const int i = lane + 32 * j;
+        if (i < n && sg[i]) xneg |= 1u << j;
+    }
+    for (int j = 0; j < PER; ++j) {
+        unsigned w = __ballot_sync(0xffffffffu, (xneg >> j) & 1u);
+        if (lane == 0) words[warp][j] = w;
+    }
+    __syncwarp();
+    double lx[PER], dg[PER];
+#pragma unroll
+    for (int j = 0; j < PER; ++j) { lx[j] = 0.0; dg[j] = 0.0; }
+    for (int k = 0; k < n; ++k) {
+        const double xk = (words[warp][k >> 5] >> (k & 31)) & 1u ? -1.0 : 1.0;
+        const double *col = L + (size_t)k * n;
+#pragma unroll
+        for (int j = 0; j < PER; ++j) {
+            const int i = lane + 32 * j;
+            if (i < n) lx[j] += col[i] * xk;
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < PER; ++j) {
+        const int i = lane + 32 * j;
+        if (i < n) dg[j] = L[i + (size_t)i * n];
+    }
+    // flip the element of largest gain (first on ties) while the gain exceeds 0.001
+    for (int it = 0; it < 16 * n + 64; ++it) {
+        double best = -kBig;
+        int idx = 0x7fffffff;
+#pragma unroll
+        for (int j = 0; j < PER; ++j) {
+            const int i = lane + 32 * j;
+            if (i >= n) continue;
+            const double xi = (xneg >> j) & 1u ? -1.0 : 1.0;
+            const double dl = dg[j] - xi * lx[j];
+            if (dl > best) { best = dl; idx = i; }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            double ob = __shfl_xor_sync(0xffffffffu, best, o);
+            int oi = __shfl_xor_sync(0xffffffffu, idx, o);
+            if (ob > best || (ob == best && oi < idx)) { best = ob; idx = oi; }
+        }
+        if (!(best > 0.001)) break;
+        const int ol = idx & 31, oj = idx >> 5;
+        const unsigned on = __shfl_sync(0xffffffffu, xneg, ol);
+        const double sgn = ((on >> oj) & 1u) ? 2.0 : -2.0;  // x = +1: Lx -= 2 L(idx, .), else +=
+        const double *col = L + (size_t)idx * n;
+#pragma unroll
+        for (int j = 0; j < PER; ++j) {
+            const int i = lane + 32 * j;
+            if (i < n) {
+                const double l = col[i];
+                if (fabs(l) > 0.001) lx[j] += sgn * l;
+            }
+        }
+        if (lane == ol) xneg ^= 1u << oj;
+    }
+    for (int j = 0; j < PER; ++j) {
+        const int i = lane + 32 * j;
+        if (i < n) sg[i] = (xneg >> j) & 1u;
+    }
+    // the full solution: free variables U[u] from element u, fixed ones from the node
+    const int *ls = lists + (size_t)si * list_stride;
+    const int nu = ls[0], nf1 = ls[1], nfx = ls[2];
+    const int *U = ls + 3, *FX = U + nu + nf1, *FS = FX + nfx;
+    __syncwarp();
+    for (int j = lane; j < PER; j += 32) words[warp][j] = 0u;
+    __syncwarp();
+    for (int j = 0; j < PER; ++j) {
+        const int u = lane + 32 * j;
+        if (u < nu && !((xneg >> j) & 1u)) atomicOr(&words[warp][U[u] >> 5], 1u << (U[u] & 31));
+    }
+    for (int f = lane; f < nfx; f += 32)
+        if (FS[f]) atomicOr(&words[warp][FX[f] >> 5], 1u << (FX[f] & 31));
+    __syncwarp();
+    const int pb = N - 1;
+    double v = 0.0;
+    for (int i = 0; i < pb; ++i) {
+        if (!((words[warp][i >> 5] >> (i & 31)) & 1u)) continue;
+        const double *row = SL + (size_t)i * N;
+        for (int j = lane; j < pb; j += 32)
+            if ((words[warp][j >> 5] >> (j & 31)) & 1u) v += row[j];
+    }
+    v = warp_sum(v);
+    if (lane == 0) hval[(size_t)q * count + h] = v;
+}
+
 inline int cdiv(size_t a, int b) { return (int)((a + b - 1) / b); }
 inline int grid_for(size_t tot) {
     int g = cdiv(tot, 256);
@@ -183,6 +294,11 @@ void launch_heur_vectors(Slot *d, const int *slots, const unsigned long long *ke
     int g = grid_for((size_t)npad * count);
     g = g > 64 ? 64 : g;
     k_heur_vec<<<dim3(g, nslots), 256, 0, st>>>(d, slots, keys, count, npad, stride, V);
+}
+void launch_heur_1opt(const Slot *d, const int *slots, int nslots, int count, int N, const int *lists, int list_stride,
+                      const double *SL, unsigned char *signs, size_t sstride, double *hval, cudaStream_t st) {
+    k_heur_1opt<<<dim3((count + 3) / 4, nslots), 128, 0, st>>>(d, slots, count, N, lists, list_stride, SL, signs,
+                                                                sstride, hval);
 }
 void launch_heur_signs(Slot *d, const int *slots, int nslots, int count, int npad, size_t stride, const float *H,
                        unsigned char *out, size_t out_stride, cudaStream_t st) {

@@ -146,6 +146,7 @@ def lib():
     L.mcb_log_fetch.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p]
     L.mcb_log_clear.argtypes = [C.c_void_p]
     L.mcb_graph_stats.argtypes = [C.c_void_p, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]
+    L.mcb_host_stats.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
     L.mcb_set_profile.argtypes = [C.c_void_p, C.c_int]
     L.mcb_library_launch_count.restype = C.c_longlong
     L.mcb_library_launch_count.argtypes = [C.c_void_p]
@@ -308,6 +309,13 @@ class Context:
 
     def launch_count(self):
         return lib().mcb_launch_count(self.h)
+
+    def host_stats(self):
+        cap = 16
+        names = (C.c_char * 32 * cap)()
+        sec = (C.c_double * cap)()
+        k = lib().mcb_host_stats(self.h, cap, C.cast(names, C.c_void_p), C.cast(sec, C.c_void_p))
+        return {bytes(names[i]).split(b"\0")[0].decode(): sec[i] for i in range(k)}
 
     def graph_stats(self):
         a, b = C.c_longlong(), C.c_longlong()
