@@ -130,9 +130,39 @@ __device__ __forceinline__ void split3(float x, __nv_bfloat16 &h, __nv_bfloat16 
     l = __float2bfloat16_rn(r - __bfloat162float(m));
 }
 
+// three BF16 pieces of four values, packed for 64-bit stores
+__device__ __forceinline__ void split3x4(float4 x, uint2 &h, uint2 &m, uint2 &l) {
+    const float xs[4] = {x.x, x.y, x.z, x.w};
+    __nv_bfloat162 hp[2], mp[2], lp[2];
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        const float a = xs[2 * k], b = xs[2 * k + 1];
+        hp[k] = __floats2bfloat162_rn(a, b);
+        const float ra = a - __low2float(hp[k]), rb = b - __high2float(hp[k]);
+        mp[k] = __floats2bfloat162_rn(ra, rb);
+        lp[k] = __floats2bfloat162_rn(ra - __low2float(mp[k]), rb - __high2float(mp[k]));
+    }
+    h = make_uint2(*reinterpret_cast<uint32_t *>(&hp[0]), *reinterpret_cast<uint32_t *>(&hp[1]));
+    m = make_uint2(*reinterpret_cast<uint32_t *>(&mp[0]), *reinterpret_cast<uint32_t *>(&mp[1]));
+    l = make_uint2(*reinterpret_cast<uint32_t *>(&lp[0]), *reinterpret_cast<uint32_t *>(&lp[1]));
+}
+
 struct Maps {
     CUtensorMap a[kPieces], b[kPieces];
 };
+
+#ifdef MCB_TC_TRACE
+__device__ unsigned long long g_tc_trace[64];
+__device__ __forceinline__ void trace(int k) {
+    if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) {
+        unsigned long long t;
+        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+        g_tc_trace[k] = t;
+    }
+}
+#else
+__device__ __forceinline__ void trace(int) {}
+#endif
 
 template <int kStages>
 __global__ void __launch_bounds__(128, 3 - kStages) k_tc_gemm(const __grid_constant__ Maps maps, TcOut out, int npad,
@@ -157,6 +187,7 @@ __global__ void __launch_bounds__(128, 3 - kStages) k_tc_gemm(const __grid_const
     const int m0 = ti * BM, n0 = tj * BN;
     const int slot = live[blockIdx.y];
     const int nk = npad / BK;
+    trace(0);
 
     if (tid == 0) {
         for (int s = 0; s < kStages; ++s) {
@@ -176,6 +207,7 @@ __global__ void __launch_bounds__(128, 3 - kStages) k_tc_gemm(const __grid_const
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = *tmem_slot;
+    trace(1);
 
     if (tid == 0) {
         const uint32_t idesc = instr_desc(BM, BN);
@@ -195,6 +227,7 @@ __global__ void __launch_bounds__(128, 3 - kStages) k_tc_gemm(const __grid_const
             const uint32_t use = (uint32_t)(kc / kStages) & 1u;
             ok = mbar_wait(&full[s], use);
             if (!ok) break;
+            trace(2 + 2 * kc);
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             const uint32_t base = smem_u32(smem + s * kStageBytes);
 #pragma unroll
@@ -214,6 +247,7 @@ __global__ void __launch_bounds__(128, 3 - kStages) k_tc_gemm(const __grid_const
             if (kc + kStages < nk) {
                 ok = mbar_wait(&empty[s], use);
                 if (!ok) break;
+                trace(3 + 2 * kc);
                 load(kc + kStages);
             }
         }
@@ -225,52 +259,108 @@ __global__ void __launch_bounds__(128, 3 - kStages) k_tc_gemm(const __grid_const
     bool ok = mbar_wait(done, 0);
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const int bad = __syncthreads_or(!ok || s_fail);
+    trace(40);
     if (bad) {
         if (tid == 0 && out.err) atomicExch(out.err, MCB_ERR_ITER);
     } else {
         const int n = nlist[blockIdx.y];
-        // 1. both accumulators -> a shared-memory tile F[r][c] (the stage buffers
-        //    are free once the MMAs have completed), rows padded to 129 floats
+        // Stores go through a shared-memory tile (the stage buffers are free once
+        // the MMAs are done) so that every global store is coalesced and 64 or
+        // 128 bits wide.  Symmetric products: the lower triangle is stored twice,
+        // as (row, col) from a row-major tile and mirrored to (col, row) from a
+        // column-major one (the accumulators are read a second time for it), so
+        // the result is exactly symmetric; diagonal tiles store their lower part.
+        constexpr int LD = BN + 4;  // 16-byte rows, conflict-free 128-bit accesses
         float *F = (float *)smem;
-        constexpr int LD = BN + 1;
         const int r = warp * 32 + lane;
+        const bool diag_tile = sym && ti == tj;
+        const size_t sb = (size_t)slot * out.stride;
+        auto value = [&](float acc, int row, int col) {
+            return alpha * acc + ((row == col && row < n) ? diag : 0.0f);
+        };
+        // store elements valid_from .. valid_to of four consecutive values (all of
+        // them as vectors); unrolled with register selects, no local memory
+        auto store4 = [&](size_t o, float4 x, int valid_from, int valid_to) {
+            if (valid_from == 0 && valid_to == 3) {
+                if (out.f32) *reinterpret_cast<float4 *>(out.f32 + o) = x;
+                if (out.f64) {
+                    reinterpret_cast<double2 *>(out.f64 + o)[0] = make_double2(x.x, x.y);
+                    reinterpret_cast<double2 *>(out.f64 + o)[1] = make_double2(x.z, x.w);
+                }
+                if (out.p[0]) {
+                    uint2 h, m, l;
+                    split3x4(x, h, m, l);
+                    *reinterpret_cast<uint2 *>(out.p[0] + o) = h;
+                    *reinterpret_cast<uint2 *>(out.p[1] + o) = m;
+                    *reinterpret_cast<uint2 *>(out.p[2] + o) = l;
+                }
+            } else {
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                    if (e < valid_from || e > valid_to) continue;
+                    const float xe = e == 0 ? x.x : (e == 1 ? x.y : (e == 2 ? x.z : x.w));
+                    if (out.f32) out.f32[o + e] = xe;
+                    if (out.f64) out.f64[o + e] = (double)xe;
+                    if (out.p[0]) {
+                        __nv_bfloat16 h, m, l;
+                        split3(xe, h, m, l);
+                        out.p[0][o + e] = h;
+                        out.p[1][o + e] = m;
+                        out.p[2][o + e] = l;
+                    }
+                }
+            }
+        };
+        // (1) row-major tile F[r][c] = C(m0 + r, n0 + c)
         for (int c0 = 0; c0 < BN; c0 += 32) {
             float v[32], w[32];
             tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
             tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(BN + c0), w);
 #pragma unroll
-            for (int j = 0; j < 32; ++j) F[r * LD + c0 + j] = v[j] + w[j];
+            for (int q = 0; q < 8; ++q) {
+                const int c = c0 + 4 * q;
+                float4 x = make_float4(value(v[4 * q] + w[4 * q], m0 + r, n0 + c),
+                                       value(v[4 * q + 1] + w[4 * q + 1], m0 + r, n0 + c + 1),
+                                       value(v[4 * q + 2] + w[4 * q + 2], m0 + r, n0 + c + 2),
+                                       value(v[4 * q + 3] + w[4 * q + 3], m0 + r, n0 + c + 3));
+                *reinterpret_cast<float4 *>(F + r * LD + c) = x;
+            }
         }
         __syncthreads();
-        // 2. coalesced stores.  Symmetric products: the lower triangle is stored
-        //    twice, as (row, col) and mirrored to (col, row), so the result is
-        //    exactly symmetric; diagonal tiles store their lower part only.
-        const size_t sb = (size_t)slot * out.stride;
-        auto put = [&](size_t o, float acc, int row, int col) {
-            const bool d = row == col && row < n;
-            const float x = alpha * acc + (d ? diag : 0.0f);
-            if (out.f32) out.f32[o] = x;
-            if (out.f64) out.f64[o] = (double)alpha * (double)acc + (d ? (double)diag : 0.0);
-            if (out.p[0]) {
-                __nv_bfloat16 h, m, l;
-                split3(x, h, m, l);
-                out.p[0][o] = h;
-                out.p[1][o] = m;
-                out.p[2][o] = l;
+        trace(42);
+        // direct half: warp per row, lane per 4 columns; diagonal tiles keep col <= row
+        for (int rr = warp; rr < BM; rr += 4) {
+            const int c = 4 * lane;
+            if (diag_tile && c > rr) continue;
+            const float4 x = *reinterpret_cast<const float4 *>(F + rr * LD + c);
+            // on a diagonal tile, columns c .. min(c + 3, rr)
+            store4(sb + (size_t)(m0 + rr) * npad + n0 + c, x, 0, diag_tile ? min(3, rr - c) : 3);
+        }
+        trace(43);
+        if (sym) {
+            __syncthreads();
+            // (2) column-major tile F[c][r] = C(m0 + r, n0 + c), from the accumulators again
+            for (int c0 = 0; c0 < BN; c0 += 32) {
+                float v[32], w[32];
+                tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+                tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(BN + c0), w);
+#pragma unroll
+                for (int j = 0; j < 32; ++j) F[(c0 + j) * LD + r] = value(v[j] + w[j], m0 + r, n0 + c0 + j);
             }
-        };
-        for (int rr = warp; rr < BM; rr += 4)
-            for (int cc = lane; cc < BN; cc += 32) {
-                if (sym && ti == tj && rr < cc) continue;
-                put(sb + (size_t)(m0 + rr) * npad + n0 + cc, F[rr * LD + cc], m0 + rr, n0 + cc);
+            __syncthreads();
+            trace(44);
+            // mirrored half: output row n0 + cc, lane per 4 rows of the tile; diagonal
+            // tiles keep rows strictly below the diagonal (rr > cc)
+            for (int cc = warp; cc < BN; cc += 4) {
+                const int rr0 = 4 * lane;
+                const int from = diag_tile ? max(0, cc + 1 - rr0) : 0;
+                if (from >= 4) continue;
+                const float4 x = *reinterpret_cast<const float4 *>(F + cc * LD + rr0);
+                store4(sb + (size_t)(n0 + cc) * npad + m0 + rr0, x, from, 3);
             }
-        if (sym)
-            for (int cc = warp; cc < BN; cc += 4)
-                for (int rr = lane; rr < BM; rr += 32) {
-                    if (ti == tj && rr <= cc) continue;
-                    put(sb + (size_t)(n0 + cc) * npad + m0 + rr, F[rr * LD + cc], m0 + rr, n0 + cc);
-                }
+        }
     }
+    trace(41);
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     if (warp == 0)
@@ -371,5 +461,11 @@ void tc_split_f64(const double *src, size_t sstride, const TcOut &out, int npad,
     g = g > 128 ? 128 : g;
     k_tc_split<double><<<dim3(g, nlive), 256, 0, st>>>(src, sstride, out, npad, d_live);
 }
+
+#ifdef MCB_TC_TRACE
+extern "C" int mcb_tc_trace(unsigned long long *out) {
+    return cudaMemcpyFromSymbol(out, g_tc_trace, sizeof(g_tc_trace)) == cudaSuccess ? 0 : -2;
+}
+#endif
 
 }  // namespace mcb

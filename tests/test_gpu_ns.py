@@ -199,7 +199,10 @@ def test_graph_replay_matches_direct_launches(gpu_lib, proj, tmp_path):
             ctx.autotune_save(path)
             ctx2 = M.Context(M.params(include_Hepta=0, use_diff=0), SL, n, batch_max=4, flags=flags)
             ctx2.autotune_load(path)
-            assert ctx2.autotune_table() == tab
+            tab2 = ctx2.autotune_table()
+            assert [(t["npad"], t["bucket"], t["variant"]) for t in tab2] == \
+                [(t["npad"], t["bucket"], t["variant"]) for t in tab]
+            assert all(abs(a - b) <= 1e-3 for t, u in zip(tab, tab2) for a, b in zip(t["us"], u["us"]))
             ctx2.close()
         ctx.close()
     assert np.array_equal(out[0][0], out[1][0]) and out[0][1] == out[1][1]
