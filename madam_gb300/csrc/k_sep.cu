@@ -199,36 +199,26 @@ __global__ void k_sa_sumx(Slot *slots, SaJob *jobs, int njobs) {
     J.sumX = sumX;
 }
 
-__global__ void __launch_bounds__(128) k_sa(Slot *slots, const SaJob *jobs, int njobs, int *perm_scratch,
-                                            int nmax, int *out_ineq, double *out_val, int total_runs) {
-    int gid = blockIdx.x * blockDim.x + threadIdx.x;
-    if (gid >= total_runs) return;
-    // locate the job (few jobs: linear scan)
-    int jb = 0;
-    while (jb + 1 < njobs && jobs[jb + 1].out_off <= gid) ++jb;
-    const SaJob &J = jobs[jb];
-    const int r = gid - J.out_off;
-    const Slot &s = slots[J.slot];
-    const int n = s.n, k = J.k;
+// The SA of one run.  The first K entries of the permutation (the k-set under
+// test) and the signs live in registers, selected by unrolled loops rather than
+// dynamic indexing (which would put them in local memory); the remaining
+// positions stay in the run's global scratch.  Terms are summed in the same
+// order as qap_simulated_annealing.c, so the results match the oracle exactly.
+template <int K>
+__device__ void sa_run(const Slot &s, const SaJob &J, int r, int *perm, int *out, double *out_val) {
+    const int n = s.n;
     const double *X = s.X;
-    int *out = out_ineq + (size_t)gid * 8;
-    if (n < k) {
-        out_val[gid] = kBig;
-        for (int a = 0; a < k; ++a) out[a] = 0;
-        return;
-    }
     const int type = r % J.ntypes + 1, trial = r / J.ntypes;
-    int e[7];
-    for (int a = 0; a < k; ++a) e[a] = a < type - 1 ? -1 : 1;
+    int e[K];
+#pragma unroll
+    for (int a = 0; a < K; ++a) e[a] = a < type - 1 ? -1 : 1;
     Stream st;
     st.key = key2(J.key, (uint64_t)(trial * 8 + type));
     st.ctr = 0;
-    int *perm = perm_scratch + (size_t)gid * nmax;
-    double t = k * k;
+    double t = K * K;
     t *= J.sumX;
     t /= (n * (n - 1));
     double cost = kBig;
-    int best[7];
     for (int i = 0; i < n; ++i) perm[i] = i;
     for (int i = n - 1; i > 0; --i) {
         int rr = st.next_int() % i;
@@ -236,13 +226,20 @@ __global__ void __launch_bounds__(128) k_sa(Slot *slots, const SaJob *jobs, int 
         perm[i] = perm[rr];
         perm[rr] = tmp;
     }
-    for (int i = 0; i < k; ++i) best[i] = perm[i];
+    int pk[K], best[K];
+#pragma unroll
+    for (int i = 0; i < K; ++i) {
+        pk[i] = perm[i];
+        best[i] = pk[i];
+    }
     double t1 = t;
     int m1 = n;
     double sol = 0;
-    for (int i = 0; i < k; ++i) {
-        sol += X[perm[i] + (size_t)perm[i] * n];
-        for (int j = i + 1; j < k; ++j) sol += 2 * (e[j] * e[i]) * X[perm[j] + (size_t)perm[i] * n];
+#pragma unroll
+    for (int i = 0; i < K; ++i) {
+        sol += X[pk[i] + (size_t)pk[i] * n];
+#pragma unroll
+        for (int j = i + 1; j < K; ++j) sol += 2 * (e[j] * e[i]) * X[pk[j] + (size_t)pk[i] * n];
     }
     int not_done = 1, sweeps = 0;
     while (not_done > 0) {
@@ -251,24 +248,28 @@ __global__ void __launch_bounds__(128) k_sa(Slot *slots, const SaJob *jobs, int 
         // its start and m1 has grown 2000-fold; real runs stop long before
         if (++sweeps > kSaMaxSweeps) break;
         for (int it = 0; it < m1; ++it) {
-            int i1 = st.next_int() % k;
+            int i1 = st.next_int() % K;
             int i2 = st.next_int() % n;
             if (i2 < i1) { int tmp = i1; i1 = i2; i2 = tmp; }
-            const int p1 = perm[i1], p2 = perm[i2];
-            double delta = 0.0;
-            for (int i = 0; i < k; ++i) {
-                const int pi = perm[i];
-                delta += (e[i] * e[i1]) * (X[pi + (size_t)n * p2] - X[pi + (size_t)n * p1]);
+            // i1 < K always; i2 may lie beyond the prefix
+            int p1 = 0, e1 = 0, p2 = 0, e2 = 0;
+#pragma unroll
+            for (int a = 0; a < K; ++a) {
+                if (a == i1) { p1 = pk[a]; e1 = e[a]; }
+                if (a == i2) { p2 = pk[a]; e2 = e[a]; }
             }
-            if (i2 < k)
-                for (int i = 0; i < k; ++i) {
-                    const int pi = perm[i];
-                    delta += (e[i] * e[i2]) * (X[pi + (size_t)n * p1] - X[pi + (size_t)n * p2]);
-                }
+            if (i2 >= K) p2 = perm[i2];
+            double delta = 0.0;
+#pragma unroll
+            for (int i = 0; i < K; ++i) delta += (e[i] * e1) * (X[pk[i] + (size_t)n * p2] - X[pk[i] + (size_t)n * p1]);
+            if (i2 < K)
+#pragma unroll
+                for (int i = 0; i < K; ++i)
+                    delta += (e[i] * e2) * (X[pk[i] + (size_t)n * p1] - X[pk[i] + (size_t)n * p2]);
             delta *= 2.0;
             double tv1 = X[p1 + (size_t)n * p1] + X[p2 + (size_t)n * p2] - 2.0 * X[p2 + (size_t)n * p1];
             double tv2 = 1.0;
-            if (i2 < k) tv2 += -2 * (e[i1] * e[i2]) + 1.0;
+            if (i2 < K) tv2 += -2 * (e1 * e2) + 1.0;
             delta += tv1 * tv2;
             if (fabs(delta) < kSaZero) delta = 0.0;
             double sol_temp = sol + delta;
@@ -282,20 +283,48 @@ __global__ void __launch_bounds__(128) k_sa(Slot *slots, const SaJob *jobs, int 
             }
             if (accept) {
                 if (fabs(delta) > 0.0001) not_done = 1;
-                perm[i1] = p2;
-                perm[i2] = p1;
+#pragma unroll
+                for (int a = 0; a < K; ++a) {
+                    if (a == i1) pk[a] = p2;
+                    if (a == i2) pk[a] = p1;
+                }
+                if (i2 >= K) perm[i2] = p1;
                 sol = sol_temp;
                 if (sol < cost) {
                     cost = sol;
-                    for (int i = 0; i < k; ++i) best[i] = perm[i];
+#pragma unroll
+                    for (int i = 0; i < K; ++i) best[i] = pk[i];
                 }
             }
         }
         t1 *= 0.6;
         m1 = (int)round(m1 * 1.1);
     }
-    out_val[gid] = cost;
-    for (int a = 0; a < k; ++a) out[a] = best[a];
+    *out_val = cost;
+#pragma unroll
+    for (int a = 0; a < K; ++a) out[a] = best[a];
+}
+
+__global__ void __launch_bounds__(128) k_sa(Slot *slots, const SaJob *jobs, int njobs, int *perm_scratch,
+                                            int nmax, int *out_ineq, double *out_val, int total_runs) {
+    int gid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= total_runs) return;
+    // locate the job (few jobs: linear scan)
+    int jb = 0;
+    while (jb + 1 < njobs && jobs[jb + 1].out_off <= gid) ++jb;
+    const SaJob &J = jobs[jb];
+    const int r = gid - J.out_off;
+    const Slot &s = slots[J.slot];
+    const int n = s.n, k = J.k;
+    int *out = out_ineq + (size_t)gid * 8;
+    if (n < k) {
+        out_val[gid] = kBig;
+        for (int a = 0; a < k; ++a) out[a] = 0;
+        return;
+    }
+    int *perm = perm_scratch + (size_t)gid * nmax;
+    if (k == 5) sa_run<5>(s, J, r, perm, out, out_val + gid);
+    else sa_run<7>(s, J, r, perm, out, out_val + gid);
 }
 
 // ---------------------------------------------------------------------------
