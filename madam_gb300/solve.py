@@ -1,0 +1,108 @@
+"""Command-line branch-and-bound in the reference's formats.
+
+Reads a rudy-format instance and a parameter file the way process_input.c does
+(readParameters, process_input.c:141-178: "name = value" lines, unknown names
+ignored, missing ones at their defaults; readData, :182-312) and writes the
+report of bab_functions.c (printFinalOutput / printSolution, :340-373), so a run
+can be diffed against the reference's .output files.  The branch-and-bound is
+the library's batched driver (mcb_bab) on the GPU.
+
+    python -m madam_gb300.solve INSTANCE PARAMS [--form learned|mixed|fp64] [--batch 64] [--out FILE]
+"""
+import argparse
+import os
+import sys
+import time
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+if os.path.dirname(HERE) not in sys.path:
+    sys.path.insert(0, os.path.dirname(HERE))
+
+from madam_gb300 import graphs as G  # noqa: E402
+from madam_gb300 import lib as M  # noqa: E402
+
+# value formats of the reference's PARAM_FIELDS (admm.h), in its order
+_FLOAT = {"sigma0", "scaleSigma", "tol0", "scaleTol", "minTol", "violated_TriIneq"}
+PARAM_ORDER = [name for name, _ in M.PARAM_FIELDS]
+
+
+def read_params(path):
+    """Parameter file -> dict over every field (defaults = the shipped file's values)."""
+    vals = dict(M.SHIPPED)
+    with open(path) as f:
+        for line in f:
+            if "=" not in line:
+                continue
+            name, _, rest = line.partition("=")
+            name = name.strip()
+            if name not in vals:
+                continue
+            tok = rest.split()
+            if not tok:
+                continue
+            try:
+                vals[name] = float(tok[0]) if name in _FLOAT else int(float(tok[0]))
+            except ValueError:
+                pass
+    return vals
+
+
+def format_params(vals):
+    lines = ["Parameters:"]
+    for name in PARAM_ORDER:
+        v = vals[name]
+        lines.append("%20s = %s" % (name, ("%f" % v) if name in _FLOAT else ("%d" % v)))
+    return "\n".join(lines)
+
+
+def report(instance, n, n_edges, vals, result, seconds):
+    """The reference's output file text for one finished run."""
+    sol = " ".join(str(i + 1) for i, x in enumerate(result["sol"]) if x == 1)
+    return "".join([
+        "Input file: %s\n" % instance,
+        "\nGraph has %d vertices and %d edges.\n" % (n, n_edges),
+        format_params(vals) + "\n",
+        "\nNodes = %d\n" % result["nodes"],
+        "Root node bound = %.2f\n" % result["root_bound"],
+        "Maximum value = %.0f\n" % result["opt"],
+        "Solution = ( %s%s)\n" % (sol, " " if sol else ""),
+        "Time = %.2f s\n\n" % seconds,
+    ])
+
+
+def solve(instance, params_path, form="mixed", batch=64, max_nodes=0):
+    n, e, w = G.read_rudy(instance)
+    vals = read_params(params_path)
+    SL = G.extended_laplacian(n, e, w).ravel(order="F")
+    flags = M.PROJ_FP64 if form == "fp64" else M.PROJ_NS_BF16
+    if form == "learned":
+        flags |= M.FLAG_LEARNED
+    ctx = M.Context(M.params(**vals), SL, n, batch_max=batch, flags=flags)
+    if form == "learned":
+        from madam_gb300 import learn as L
+        from madam_gb300 import train_models as T
+
+        ctx.set_models(*L.load(T.OUT))
+    t0 = time.perf_counter()
+    r = ctx.bab(batch=batch, max_nodes=max_nodes)
+    secs = time.perf_counter() - t0
+    ctx.close()
+    return report(instance, n, len(w), vals, r, secs), r
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("instance")
+    ap.add_argument("params")
+    ap.add_argument("--form", default="mixed", choices=["learned", "mixed", "fp64"])
+    ap.add_argument("--batch", type=int, default=64)
+    ap.add_argument("--out", default=None, help="report file (default: INSTANCE.output)")
+    a = ap.parse_args(argv)
+    text, _ = solve(a.instance, a.params, a.form, a.batch)
+    sys.stdout.write(text)
+    with open(a.out or a.instance + ".output", "w") as f:
+        f.write(text)
+
+
+if __name__ == "__main__":
+    main()

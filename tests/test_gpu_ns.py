@@ -206,3 +206,25 @@ def test_graph_replay_matches_direct_launches(gpu_lib, proj, tmp_path):
             ctx2.close()
         ctx.close()
     assert np.array_equal(out[0][0], out[1][0]) and out[0][1] == out[1][1]
+
+
+def test_solve_command_line_reaches_reference_optimum(gpu_lib, tmp_path):
+    """madam_gb300.solve: rudy instance + parameter file in, the reference's
+    report out, with the reference's optimum and a solution that attains it."""
+    import re
+
+    from madam_gb300 import solve as S
+
+    fx = FIXTURES[0]
+    n, e, w = G.gnp(*fx["args"][:3], seed=fx["args"][3])
+    inst = tmp_path / "g.rudy"
+    G.write_rudy(str(inst), n, e, w)
+    prm = tmp_path / "params"
+    prm.write_text("".join("%s = %s\n" % kv for kv in gpu_lib.SHIPPED.items()))
+    text, r = S.solve(str(inst), str(prm), form="mixed", batch=8)
+    assert r["opt"] == fx["opt"]
+    assert float(re.search(r"^Maximum value = (\S+)", text, re.M).group(1)) == fx["opt"]
+    sol = [int(v) - 1 for v in re.search(r"^Solution = \( (.*)\)", text, re.M).group(1).split()]
+    side = np.zeros(n, dtype=np.int32)
+    side[sol] = 1
+    assert G.cut_value(n, e, w, side) == fx["opt"]

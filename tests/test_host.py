@@ -131,3 +131,30 @@ def test_sharded_branch_and_bound_on_two_gloo_ranks(orc):
     assert bests == {serial["opt"]}
     assert any(r[4] == serial["opt"] for r in res)
     assert res[0][3] == res[1][3]
+
+
+# ---- reference-format command line (madam_gb300/solve.py) ----------------------
+def test_solve_reads_parameter_files(tmp_path):
+    import re
+
+    from madam_gb300 import lib as M
+    from madam_gb300 import solve as S
+
+    p = tmp_path / "params"
+    p.write_text("sigma0 = 1.6\nscaleSigma=1.002\n  unknown_name = 7\nTriIneq = 1500   \nminTol = 1e-4\n")
+    v = S.read_params(str(p))
+    assert v["sigma0"] == 1.6 and v["scaleSigma"] == 1.002 and v["TriIneq"] == 1500 and v["minTol"] == 1e-4
+    assert all(v[k] == M.SHIPPED[k] for k in M.SHIPPED if k not in ("sigma0", "scaleSigma", "TriIneq", "minTol"))
+    ref = "/root/reference/params"
+    if os.path.exists(ref):
+        assert S.read_params(ref) == {k: type(M.SHIPPED[k])(v) for k, v in M.SHIPPED.items()}
+    # the report parses like the reference's .output files
+    res = dict(nodes=41, root_bound=1447.82190427, opt=1435.0, sol=[1, 0, 0, 1, 1])
+    txt = S.report("g.rudy", 6, 9, v, res, 12.345)
+    assert re.search(r"^Maximum value = (\S+)", txt, re.M).group(1) == "1435"
+    assert re.search(r"^Root node bound = (\S+)", txt, re.M).group(1) == "1447.82"
+    assert re.search(r"^Nodes = (\d+)", txt, re.M).group(1) == "41"
+    assert re.search(r"^Solution = \( (.*)\)", txt, re.M).group(1).split() == ["1", "4", "5"]
+    assert re.search(r"sigma0 = (\S+)", txt).group(1) == "1.600000"
+    assert re.search(r"^Time = (\S+) s", txt, re.M).group(1) == "12.35"
+    assert "Graph has 6 vertices and 9 edges." in txt
