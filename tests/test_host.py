@@ -158,3 +158,15 @@ def test_solve_reads_parameter_files(tmp_path):
     assert re.search(r"sigma0 = (\S+)", txt).group(1) == "1.600000"
     assert re.search(r"^Time = (\S+) s", txt, re.M).group(1) == "12.35"
     assert "Graph has 6 vertices and 9 edges." in txt
+
+
+@pytest.mark.skipif(not os.path.isdir("/root/reference"), reason="reference headers not present")
+def test_reference_shim_compiles_against_the_reference_headers():
+    """The C binding a maintainer adds to MADAM (madam_gb300/shim) compiles against
+    the reference's admm.h (with the oracle's single-rank mpi.h) and mcbound.h."""
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run(["gcc", "-std=gnu11", "-Wall", "-Werror", "-fsyntax-only", "-I/root/reference",
+                        "-I" + os.path.join(root, "oracle", "ref"), "-I" + os.path.join(root, "include"),
+                        os.path.join(root, "madam_gb300", "shim", "mcb_madam_shim.c")],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
