@@ -311,7 +311,7 @@ def run_ours(a):
         SLt = G.extended_laplacian(n, e, w).ravel(order="F")
         tto = {"instance": "G(%d, %.1f) %s weights seed %d, triangle cuts, batch 64" % (
             TTO["n"], TTO["p"], TTO["weights"], TTO["seed"])}
-        for form in (a.form, "fp64"):
+        for form in ((a.form, "mixed", "fp64") if a.form == "learned" else (a.form, "fp64")):
             tc = _context(M, M.params(**TTO["params"]), SLt, n, 64, form, profile=False)
             torch.cuda.synchronize()
             t0 = time.perf_counter()
