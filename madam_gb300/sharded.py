@@ -9,6 +9,13 @@ lower bound after every batch (MADAM pushes NEW_VALUE to its master,
 bab_functions.c:242-256), plus a sum-allreduce of queue sizes to detect global
 termination.  No matrix data crosses ranks, so there is no device collective.
 
+When a rank's queue runs dry while another holds two or more open nodes, the
+ranks rebalance: every rank learns all queue sizes (an all-gather of one integer),
+computes the same transfer plan from them (each empty rank takes half of the
+currently largest queue), and the donors ship the fixings and bounds of their best
+open nodes (an all-gather of small lists).  This plays the role of the
+reference's master handing idle workers new subproblems (bab_functions.c:297-325).
+
 `ctx` is any object with evaluate(node, rank) -> (bound, stats), set_lb(lb, sol),
 lb() -> (lb, sol) and an `N` attribute; `new_node(fixed)` builds a node with
 xfixed / sol / fracsol arrays (the BabNode layout).
@@ -34,8 +41,30 @@ def _fixed(nd, pb):
     return {i: int(nd.sol[i]) for i in range(pb) if nd.xfixed[i]}
 
 
-def sharded_bab(ctx, new_node, dist=None, depth=2, max_nodes=100000):
-    """Returns (optimum, solution vector, nodes evaluated on this rank, evaluated on all ranks)."""
+def balance_plan(sizes):
+    """Transfers [(donor, receiver, count)] that give every empty queue half of the
+    currently largest non-empty one (donors are ranks that held nodes before the
+    round, so every transfer comes out of a queue that exists); the same on every
+    rank (a function of the sizes only)."""
+    left = {d: c for d, c in enumerate(sizes) if c > 0}
+    plan = []
+    for r, c in enumerate(sizes):
+        if c != 0:
+            continue
+        if not left:
+            break
+        d = max(left, key=lambda k: (left[k], -k))
+        if left[d] < 2:
+            break
+        k = left[d] // 2
+        plan.append((d, r, k))
+        left[d] -= k
+    return plan
+
+
+def sharded_bab(ctx, new_node, dist=None, depth=2, max_nodes=100000, balance=True, info=None):
+    """Returns (optimum, solution vector, nodes evaluated on this rank, evaluated on all ranks).
+    info (a dict, optional) receives the number of rebalancing transfers and nodes moved."""
     rank = dist.get_rank() if dist else 0
     world = dist.get_world_size() if dist else 1
     pb = ctx.N - 1
@@ -85,6 +114,7 @@ def sharded_bab(ctx, new_node, dist=None, depth=2, max_nodes=100000):
     heap = [(-b, next(tie), fx, new_node(fx)) for b, fx in mine]
     heapq.heapify(heap)
     local = 0
+    transfers = moved = 0
     while True:
         g = allreduce(lb, MAX)
         if g > lb:
@@ -93,6 +123,25 @@ def sharded_bab(ctx, new_node, dist=None, depth=2, max_nodes=100000):
         active = allreduce(float(len(heap)), SUM)
         if active == 0 or local >= max_nodes:
             break
+        if dist and balance and world > 1:
+            sizes = [None] * world
+            dist.all_gather_object(sizes, len(heap))
+            plan = balance_plan(sizes)
+            if plan:
+                out = []
+                for d, r, k in plan:
+                    if d == rank:
+                        for _ in range(k):
+                            negb, _, fx, _ = heapq.heappop(heap)
+                            out.append((r, -negb, fx))
+                got = [None] * world
+                dist.all_gather_object(got, out)
+                for lst in got:
+                    for r, b, fx in lst:
+                        if r == rank:
+                            heapq.heappush(heap, (-b, next(tie), fx, new_node(fx)))
+                transfers += len(plan)
+                moved += sum(k for _, _, k in plan)
         if heap:
             negb, _, fx, nd = heapq.heappop(heap)
             if lb + 1.0 < -negb:
@@ -109,5 +158,7 @@ def sharded_bab(ctx, new_node, dist=None, depth=2, max_nodes=100000):
                         heapq.heappush(heap, (-b, next(tie), f2, new_node(f2)))
     best = allreduce(lb, MAX)
     total = allreduce(float(local + evaluated), SUM)
+    if info is not None:
+        info.update(transfers=transfers, moved=moved)
     own = np.asarray(sol)[:pb] if lb == best else None
     return best, own, local + evaluated, int(total)

@@ -91,7 +91,7 @@ def test_bench_reference_arm_prints_one_json_line():
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["cpu_baseline"]["kind"] == "port"
 
 
-def _sharded_worker(rank, world, port, q):
+def _sharded_worker(rank, world, port, q, depth=2):
     import torch.distributed as dist
 
     os.environ["MASTER_ADDR"] = "127.0.0.1"
@@ -105,18 +105,22 @@ def _sharded_worker(rank, world, port, q):
     n, e, w = G2.gnp(64, 0.5, "pm1", seed=13)
     SL = O.build_L(n, (e, w))
     ctx = O.Ctx(O.shipped_params(), SL, n)
-    best, sol, mine, total = sharded_bab(ctx, lambda fx: O.make_node(n - 1, fx), dist=dist, depth=2)
-    q.put((rank, best, mine, total, None if sol is None else G2.cut_value(n, e, w, sol)))
+    info = {}
+    best, sol, mine, total = sharded_bab(ctx, lambda fx: O.make_node(n - 1, fx), dist=dist, depth=depth, info=info)
+    q.put((rank, best, mine, total, None if sol is None else G2.cut_value(n, e, w, sol), info))
     dist.destroy_process_group()
 
 
-def test_sharded_branch_and_bound_on_two_gloo_ranks(orc):
+@pytest.mark.parametrize("world,depth", [(2, 2), (3, 1)])
+def test_sharded_branch_and_bound_on_gloo_ranks(orc, world, depth):
+    """Ranks expand the top of the tree, deal the frontier, rebalance when a queue
+    runs dry, and agree on the serial optimum."""
     import torch.multiprocessing as mp
 
     ctx = mp.get_context("spawn")
     q = ctx.Queue()
-    port = 29500 + os.getpid() % 1000
-    ps = [ctx.Process(target=_sharded_worker, args=(r, 2, port, q)) for r in range(2)]
+    port = 29500 + (os.getpid() + 7 * world) % 1000
+    ps = [ctx.Process(target=_sharded_worker, args=(r, world, port, q, depth)) for r in range(world)]
     for p in ps:
         p.start()
     res = [q.get(timeout=600) for _ in ps]
@@ -130,7 +134,19 @@ def test_sharded_branch_and_bound_on_two_gloo_ranks(orc):
     bests = {r[1] for r in res}
     assert bests == {serial["opt"]}
     assert any(r[4] == serial["opt"] for r in res)
-    assert res[0][3] == res[1][3]
+    assert len({r[3] for r in res}) == 1
+    if world == 3:  # one of three ranks starts with an empty queue (a frontier of two nodes)
+        assert res[0][5]["transfers"] >= 1 and res[0][5]["moved"] >= 1
+
+
+def test_balance_plan():
+    from madam_gb300.sharded import balance_plan
+
+    assert balance_plan([5, 0, 3]) == [(0, 1, 2)]
+    assert balance_plan([0, 0, 6]) == [(2, 0, 3), (2, 1, 1)]
+    assert balance_plan([0, 8, 0, 2]) == [(1, 0, 4), (1, 2, 2)]
+    assert balance_plan([1, 0, 1]) == []
+    assert balance_plan([4, 4]) == []
 
 
 # ---- reference-format command line (madam_gb300/solve.py) ----------------------
