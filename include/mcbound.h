@@ -134,6 +134,9 @@ int mcb_ns_options(mcb_ctx *ctx, int operands, double l0);
 /* the Newton-Schulz step schedule of the context: count, and per step a, b of
  * S <- a S + b S^3 and whether its operands are FP32-accurate */
 int mcb_ns_schedule(const mcb_ctx *ctx, int cap, float *a, float *b, int *accurate);
+/* the default schedule (safety 2%, closing within 1e-7 of 1) for a given l0; host
+ * arithmetic only, callable without a device.  Returns the step count or MCB_ERR_ARG. */
+int mcb_ns_schedule_for(double l0, int cap, float *a, float *b, int *accurate);
 
 /* ---- the bound ---------------------------------------------------------------
  * mcb_evaluate: Evaluate(node, SP, PP, rank) (evaluate.c:12).  Writes

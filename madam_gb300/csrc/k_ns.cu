@@ -333,6 +333,22 @@ std::vector<NsStep> ns_schedule(double l0, double safety, double eps) {
     return st;
 }
 
+}  // namespace mcb
+
+// the step schedule for a given l0 (host arithmetic only; no device needed)
+extern "C" int mcb_ns_schedule_for(double l0, int cap, float *a, float *b, int *accurate) {
+    if (!(l0 > 0.0 && l0 < 0.5)) return MCB_ERR_ARG;
+    std::vector<mcb::NsStep> st = mcb::ns_schedule(l0, 0.02, 1e-7);
+    for (int k = 0; k < (int)st.size() && k < cap; ++k) {
+        if (a) a[k] = st[k].a;
+        if (b) b[k] = st[k].b;
+        if (accurate) accurate[k] = st[k].accurate;
+    }
+    return (int)st.size();
+}
+
+namespace mcb {
+
 int NsProj::init(int form_, int nmax_, int cap_, cudaStream_t st) {
     form = form_;
     nmax = nmax_;

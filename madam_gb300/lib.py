@@ -150,6 +150,7 @@ def lib():
     L.mcb_set_profile.argtypes = [C.c_void_p, C.c_int]
     L.mcb_library_launch_count.restype = C.c_longlong
     L.mcb_library_launch_count.argtypes = [C.c_void_p]
+    L.mcb_ns_schedule_for.argtypes = [C.c_double, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
     L.mcb_split_gemm.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_float, C.c_float, C.c_int,
                                  C.c_int, C.c_void_p]
     L.mcb_autotune_table.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
@@ -437,6 +438,16 @@ def project_noalloc(n, W_dev, Xp_dev, Q_dev, Z_dev, evals_dev, stream=None):
                                          C.c_void_p(Z_dev), C.c_void_p(evals_dev), C.byref(M),
                                          None if stream is None else C.c_void_p(stream)))
     return M.value
+
+
+def ns_schedule_for(l0=1e-6):
+    """The Newton-Schulz step schedule (a, b, FP32-accurate) for l0; needs no device."""
+    cap = 64
+    a, b, acc = (C.c_float * cap)(), (C.c_float * cap)(), (C.c_int * cap)()
+    k = lib().mcb_ns_schedule_for(l0, cap, C.cast(a, C.c_void_p), C.cast(b, C.c_void_p), C.cast(acc, C.c_void_p))
+    if k < 0:
+        _check(k)
+    return [(a[i], b[i], acc[i]) for i in range(min(k, cap))]
 
 
 def split_gemm(A, B, alpha=1.0, diag=0.0, sym=False, variant=0):

@@ -186,3 +186,36 @@ def test_reference_shim_compiles_against_the_reference_headers():
                         os.path.join(root, "madam_gb300", "shim", "mcb_madam_shim.c")],
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def test_newton_schulz_schedule_against_a_restatement():
+    """The library's step schedule (host arithmetic, no device) is the scaled
+    Newton-Schulz iteration of Chen & Chow: k^2 = 3 (1 - 0.02) / (1 + l + l^2),
+    p(x) = 1.5 k x - 0.5 (k x)^3, until 1 - l < 1e-7, FP32-accurate from l > 0.9,
+    and at least two accurate closing steps.  Every step keeps [0, 1] inside [0, 1]."""
+    from madam_gb300 import build as B
+    from madam_gb300 import lib as M
+
+    if not os.path.exists(M.LIB_PATH):
+        B.build()
+    for l0 in (1e-3, 1e-6, 1e-9):
+        st = M.ns_schedule_for(l0)
+        l, ref = l0, []
+        while 1 - l > 1e-7 and len(ref) < 64:
+            k2 = 3 * 0.98 / (1 + l + l * l)
+            k = np.sqrt(k2) if k2 > 1 else 1.0
+            ref.append((1.5 * k, -0.5 * k ** 3, int(l > 0.9)))
+            p = lambda y: 1.5 * y - 0.5 * y ** 3
+            l = min(p(k * l), p(k))
+        while sum(r[2] for r in ref) < 2:
+            ref.append((1.5, -0.5, 1))
+        assert len(st) == len(ref)
+        assert np.allclose([s[0] for s in st], [r[0] for r in ref], rtol=1e-6)
+        assert np.allclose([s[1] for s in st], [r[1] for r in ref], rtol=1e-6)
+        assert [s[2] for s in st] == [r[2] for r in ref]
+        xs = np.linspace(0, 1, 4001)
+        for a, b, _ in st:
+            y = a * xs + b * xs ** 3
+            assert y.min() >= -1e-7 and y.max() <= 1 + 1e-6
+    with pytest.raises(M.MCBError):
+        M.ns_schedule_for(0.6)
