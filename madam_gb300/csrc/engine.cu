@@ -462,7 +462,7 @@ int run_chunk(mcb_ctx *c, int ns, int mmax, int emax, int chunk) {
             if (int rc = launch_admm_iteration(c, ns, mmax, emax)) return rc;
         return MCB_OK;
     }
-    std::vector<int> key{ns, mmax, emax, chunk, c->proj, c->ns.npad, c->ns.live, c->ns.variant};
+    std::vector<int> key{ns, mmax, emax, chunk, c->proj, c->ns.npad, c->ns.live, c->ns.variant, c->ns.version};
     if (!c->gexec || key != c->gkey) {
         long long l0[K_NCLASS];
         double w0[K_NCLASS];

@@ -384,6 +384,7 @@ int NsProj::configure(int operands_, double l0_) {
     operands = operands_;
     l0 = l0_;
     steps = ns_schedule(l0, 0.02, 1e-7);
+    ++version;
     return MCB_OK;
 }
 

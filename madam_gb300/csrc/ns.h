@@ -60,6 +60,7 @@ struct NsProj {
     };
     std::map<std::pair<int, int>, Tuned> tuned;
     int variant = 0;                // variant of the current launch configuration
+    int version = 0;                // bumped when the schedule or operands change (graph keys)
     static int bucket(int nlive) {
         int b = 1;
         while (b < nlive) b <<= 1;
