@@ -198,3 +198,33 @@ def test_mlp_restatement_gradient_against_finite_differences():
         e[q] = eps
         num[q] = (R.loss_and_grad(p + e, X, Y, d, h1, h2)[0] - R.loss_and_grad(p - e, X, Y, d, h1, h2)[0]) / (2 * eps)
     assert np.allclose(g, num, rtol=1e-6, atol=1e-8)
+
+
+def test_scaled_newton_schulz_projection_in_float64():
+    """The chosen form's algorithm, restated in numpy float64: W / ||W||_F through
+    the library's step schedule gives sign(W), and (W + W S) / 2 matches the
+    eigendecomposition projection up to the unresolved band |lambda| < l0 ||W||_F."""
+    from madam_gb300 import build as B
+    from madam_gb300 import lib as M
+
+    if not os.path.exists(M.LIB_PATH):
+        B.build()
+    rng = np.random.default_rng(11)
+    n = 120
+    A = rng.standard_normal((n, n))
+    W = (A + A.T) / np.sqrt(2 * n)
+    w, V = np.linalg.eigh(W)
+    Xr = (V[:, w > 0] * w[w > 0]) @ V[:, w > 0].T
+    for l0 in (1e-3, 1e-6):
+        S = W / np.linalg.norm(W)
+        for a, b, _ in M.ns_schedule_for(l0):
+            S = a * S + b * (S @ S @ S)
+        X = 0.5 * (W + W @ S)
+        err = np.linalg.norm(X - Xr) / np.linalg.norm(W)
+        # eigenvalues below l0 ||W||_F are the only ones left unresolved
+        band = np.abs(w) < l0 * np.linalg.norm(W)
+        bound = 0.5 * np.sqrt(np.sum(w[band] ** 2)) / np.linalg.norm(W) + 1e-9
+        assert err <= max(bound, 1e-9), (l0, err, bound)
+        # M = round((n + tr S) / 2) counts the positive eigenvalues, up to the unresolved band
+        Mns = int(round(0.5 * (n + np.trace(S))))
+        assert abs(Mns - int((w > 0).sum())) <= band.sum()
