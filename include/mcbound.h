@@ -44,8 +44,10 @@ enum mcb_status {
 
 /* Projection forms (mcb_create flags, low byte) */
 #define MCB_PROJ_FP64 0x0      /* plain: FP64 tridiagonal eigensolver (dsyevr's method) */
-#define MCB_PROJ_NS_BF16 0x1   /* chosen: BF16 Newton-Schulz sign iteration + FP64 refinement */
-#define MCB_PROJ_NS_TF32 0x2   /* chosen: TF32 Newton-Schulz sign iteration + FP64 refinement */
+#define MCB_PROJ_NS_BF16 0x1   /* chosen: Newton-Schulz sign iteration on the tensor cores (tcgen05, operands
+                                  as three BF16 pieces: FP32-accurate), FP64 assembly and safe bound */
+#define MCB_PROJ_NS_TF32 0x2   /* chosen: as MCB_PROJ_NS_BF16; with MCB_NS_OPERANDS_NATIVE its one-pass
+                                  steps use TF32 operands (cuBLAS) instead of BF16 */
 /* Other flags */
 #define MCB_FLAG_PROFILE 0x100 /* time every kernel class with CUDA events */
 /* operands of the Newton-Schulz growth steps (mcb_ns_options) */
