@@ -12,11 +12,14 @@
 // maps both ends of the interval to the same value and so raises l fastest.
 // The schedule starts from l0 (eigenvalues below l0 * alpha in magnitude are
 // not resolved; they change X+ by at most l0 * alpha / 2 each) and ends once
-// 1 - l < 1e-7.  The growth steps run in the form's low precision (BF16 or TF32
-// operands), the last steps (l > 0.9, quadratic convergence) with FP32-accurate
-// operands, which removes the low-precision rounding from every resolved
-// eigen-direction.  The final product W * S runs in FP64 and the epilogue forms
-// X+ = (W + (WS + SW)/2) / 2 and Q = X+ - W in FP64.
+// 1 - l < 1e-7.  By default (MCB_NS_OPERANDS_SPLIT) every product runs on the
+// library's tcgen05 kernel (k_tc.cu) with operands carried as three BF16 pieces,
+// which is FP32-accurate: one pass of BF16 or TF32 operands cannot resolve
+// eigenvalues below its rounding (~1e-3 of alpha).  The cuBLAS modes (NATIVE:
+// one-pass growth steps and FP32-accurate closing steps, l > 0.9; FP32;
+// CUBLAS_SPLIT) are kept as reference points.  G = W S leaves the accumulators
+// as FP64 (a cuBLAS DGEMM in the cuBLAS modes) and the epilogue forms
+// X+ = (W + (G + G^T)/2) / 2 and Q = X+ - W in FP64.
 #pragma once
 #include <cublas_v2.h>
 #include <cuda_bf16.h>
