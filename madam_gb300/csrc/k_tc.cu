@@ -13,17 +13,22 @@
 // hold 24 significant bits.  The product keeps the six piece products whose
 // weight is at least 2^-16 of the leading one -- hi.hi, hi.mid, mid.hi, mid.mid,
 // hi.lo, lo.hi -- and accumulates them in FP32 in tensor memory (hi.hi and the
-// five corrections in two accumulators), so C is FP32-accurate.  The epilogue writes C as FP32, as its own three pieces (the
-// next step's operands) and/or as FP64.
+// five corrections in two accumulators), so C is FP32-accurate.  The epilogue
+// writes C as FP32, as its own three pieces (the next step's operands) and/or
+// widened to FP64.
 //
 // Tiling: one CTA per 128 x 128 tile of C and slot; K in chunks of 64 BF16
 // (one 128-byte swizzle row).  A stage holds the three pieces of the A and B
-// chunks (96 KB); with one stage per CTA two CTAs fit on an SM (shared memory
-// and the 512 tensor-memory columns), so one CTA's TMA loads overlap the other's
-// MMAs and a 64-slot batch of 256 x 256 products runs in one wave.  One thread
-// issues the TMA copies and the MMAs; all four warps drain the accumulators (32
-// lanes each) with tcgen05.ld, through a shared-memory tile for coalesced stores.  Every wait on an mbarrier is
-// bounded: on expiry the CTA records an error code and skips the rest.
+// chunks (96 KB).  Two variants, timed by the autotuner: one stage per CTA, so
+// that two CTAs fit on an SM (shared memory and the 512 tensor-memory columns)
+// and one CTA's TMA loads overlap the other's MMAs; or two stages with one CTA
+// per SM.  One thread issues the TMA copies and the MMAs; all four warps drain
+// the accumulators (32 lanes each) with tcgen05.ld, through shared-memory tiles
+// (row-major for the direct half, column-major for the mirror) so that every
+// global store is coalesced and 64 or 128 bits wide.  Every wait on an
+// mbarrier is bounded: on expiry the CTA records an error code and skips the
+// rest.  Compiled with MCB_TC_TRACE, CTA (0, 0) records globaltimer stamps of
+// its phases (read by mcb_tc_trace) for latency studies.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
