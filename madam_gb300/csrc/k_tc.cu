@@ -33,6 +33,7 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstdint>
 #include <cstring>
 
@@ -431,14 +432,19 @@ int tc_gemm(const void *amaps, const void *bmaps, const TcOut &out, int npad, in
             const int *d_n, float alpha, float diag, cudaStream_t st, int sym, int variant) {
     if (nlive <= 0) return MCB_OK;
     if (npad % BM || npad % BK || variant < 0 || variant >= kTcVariants) return MCB_ERR_ARG;
-    static bool attr = false;
-    if (!attr) {
+    // the shared-memory limit is a per-device function attribute: set it once on
+    // every device that launches the kernel
+    static std::atomic<unsigned long long> attr_set{0};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return MCB_ERR_CUDA;
+    const unsigned long long bit = (dev >= 0 && dev < 64) ? 1ull << dev : 0ull;
+    if (!bit || !(attr_set.load() & bit)) {
         if (cudaFuncSetAttribute(k_tc_gemm<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes(1)) !=
                 cudaSuccess ||
             cudaFuncSetAttribute(k_tc_gemm<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes(2)) !=
                 cudaSuccess)
             return MCB_ERR_CUDA;
-        attr = true;
+        attr_set.fetch_or(bit);
     }
     Maps m;
     memcpy(m.a, amaps, sizeof(m.a));

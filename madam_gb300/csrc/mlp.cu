@@ -12,6 +12,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -224,10 +225,15 @@ void mlp_forward_device(const MlpImpl *M, const float *dX, int n, float *dOut, c
 int mlp_step_device(MlpImpl *M, const float *dX, const float *dY, const int *dIdx, int n, float lr, cudaStream_t st) {
     const int nblk = (n + kTile - 1) / kTile;
     const size_t sm = grad_smem(M->D);
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(k_mlp_grad, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        attr = true;
+    // per-device function attribute, set once on every device that trains
+    static std::atomic<unsigned long long> attr_set{0};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return MCB_ERR_CUDA;
+    const unsigned long long bit = (dev >= 0 && dev < 64) ? 1ull << dev : 0ull;
+    if (!bit || !(attr_set.load() & bit)) {
+        if (cudaFuncSetAttribute(k_mlp_grad, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess)
+            return MCB_ERR_CUDA;
+        attr_set.fetch_or(bit);
     }
     k_mlp_grad<<<nblk, kTile, sm, st>>>(M->p, M->D, dX, dY, dIdx, n, n, M->gpart, M->lpart);
     if (lr > 0.0f) M->step++;
