@@ -22,6 +22,10 @@ WORKLOADS = {
     # G(n=512, density 10%), integer weights in [-10,10]
     "gnp512_int10": dict(n=512, p=0.1, weights="int10", seed=1401, nodes=64, max_fixed=20,
                          params=dict(use_diff=0)),
+    # 2D toroidal spin glass, 20 x 20 grid (n = 400, degree 4), weights in {-1,+1};
+    # all three cut families
+    "torus20x20_pm1": dict(kind="torus", rows=20, cols=20, seed=1301, nodes=64, max_fixed=20,
+                           params=dict(use_diff=0)),
 }
 
 
@@ -54,7 +58,10 @@ def one_opt_lb(n, edges, w, restarts=64, seed=0):
 
 def make(name):
     cfg = WORKLOADS[name]
-    n, e, w = G.gnp(cfg["n"], cfg["p"], cfg["weights"], seed=cfg["seed"])
+    if cfg.get("kind") == "torus":
+        n, e, w = G.torus2d(cfg["rows"], cfg["cols"], seed=cfg["seed"])
+    else:
+        n, e, w = G.gnp(cfg["n"], cfg["p"], cfg["weights"], seed=cfg["seed"])
     SL = G.extended_laplacian(n, e, w).ravel(order="F")
     fix = G.random_fixings(n, cfg["nodes"], cfg["max_fixed"], seed=cfg["seed"] + 7)
     lb, side = one_opt_lb(n, e, w, seed=cfg["seed"] + 3)

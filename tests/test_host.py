@@ -76,9 +76,12 @@ def test_params_and_node_layout_match_the_reference():
 def test_workload_is_deterministic():
     from madam_gb300 import workload as W
 
-    a, b = W.make("gnp100_one_tri"), W.make("gnp100_one_tri")
-    assert np.array_equal(a["SL"], b["SL"]) and a["fixings"] == b["fixings"] and a["lb"] == b["lb"]
-    assert G.cut_value(a["n"], a["edges"], a["weights"], a["lb_sol"]) == a["lb"]
+    for name in ("gnp100_one_tri", "torus20x20_pm1"):
+        a, b = W.make(name), W.make(name)
+        assert np.array_equal(a["SL"], b["SL"]) and a["fixings"] == b["fixings"] and a["lb"] == b["lb"]
+        assert G.cut_value(a["n"], a["edges"], a["weights"], a["lb_sol"]) == a["lb"]
+    t = W.make("torus20x20_pm1")
+    assert t["n"] == 400 and len(t["weights"]) == 800 and set(np.unique(t["weights"])) == {-1.0, 1.0}
 
 
 def test_bench_reference_arm_prints_one_json_line():
