@@ -83,3 +83,38 @@ def test_batch_is_order_independent(gpu_lib):
         res.append({i: b[k] for k, i in enumerate(order)})
     for i in range(6):
         assert res[0][i] == res[1][i]
+
+
+def _fixtures():
+    import json
+    import os
+
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "reference_bab.json")
+    return json.load(open(path))["instances"]
+
+
+@pytest.mark.parametrize("fx", _fixtures(), ids=lambda f: f["name"])
+def test_plain_branch_and_bound_against_reference_trees(gpu_lib, orc, fx):
+    """Whole trees of the plain FP64 form (one node per launch) on the reference's
+    fixtures: the reference's optimum, the oracle's node count in counter-stream
+    mode, and the reference's optimal cut wherever the oracle's counter mode finds
+    that same cut.  Where the optimum has ties (the +-1 torus) the rounding
+    heuristic's random stream picks among them: there the cut is checked by its value."""
+    if fx["kind"] == "gnp":
+        n, e, w = G.gnp(*fx["args"][:3], seed=fx["args"][3])
+    else:
+        n, e, w = G.torus2d(fx["args"][0], fx["args"][1], seed=fx["args"][2])
+    SL = G.extended_laplacian(n, e, w).ravel(order="F")
+    oc = orc.Ctx(orc.shipped_params(), SL, n, rng=orc.RNG_COUNTER, topk=orc.TOPK_CANONICAL, canon_sign=1)
+    ro = oc.bab(max_nodes=2000)
+    ctx = gpu_lib.Context(gpu_lib.params(), SL, n, batch_max=1, flags=gpu_lib.PROJ_FP64)
+    r = ctx.bab(batch=1, max_nodes=2000)
+    ctx.close()
+    assert r["opt"] == fx["opt"] == ro["opt"]
+    assert r["nodes"] == ro["nodes"]
+    got = sorted(np.nonzero(r["sol"])[0].tolist())
+    if sorted(np.nonzero(ro["sol"])[0].tolist()) == sorted(fx["sol"]):
+        assert got == sorted(fx["sol"])
+    side = np.zeros(n, dtype=np.int32)
+    side[: n - 1] = r["sol"]
+    assert G.cut_value(n, e, w, side) == fx["opt"]
