@@ -56,6 +56,25 @@ def one_opt_lb(n, edges, w, restarts=64, seed=0):
     return G.cut_value(n, edges, w, side), side
 
 
+def uneven_specs(count=2000, seed=1501):
+    """Independent subproblems of uneven size, as (n, p, weights, seed) tuples:
+    n uniform in [60, 400], density uniform in [0.1, 0.9], weights {-1,+1} or
+    integers in [-10, 10] by a fair coin per instance.  The graphs themselves are
+    drawn one at a time by uneven_instance (2000 of them hold ~0.4 GB as edge lists)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    n = rng.integers(60, 401, size=count)
+    p = rng.uniform(0.1, 0.9, size=count)
+    coin = rng.integers(0, 2, size=count)
+    return [(int(n[i]), float(p[i]), "pm1" if coin[i] == 0 else "int10", seed * 10000 + i) for i in range(count)]
+
+
+def uneven_instance(spec):
+    """One subproblem of uneven_specs: (n, edges, weights, SL column-major)."""
+    n, p, weights, s = spec
+    n, e, w = G.gnp(n, p, weights, seed=s)
+    return n, e, w, G.extended_laplacian(n, e, w).ravel(order="F")
+
+
 def make(name):
     cfg = WORKLOADS[name]
     if cfg.get("kind") == "torus":

@@ -84,6 +84,22 @@ def test_workload_is_deterministic():
     assert t["n"] == 400 and len(t["weights"]) == 800 and set(np.unique(t["weights"])) == {-1.0, 1.0}
 
 
+def test_uneven_batch_generator():
+    from madam_gb300 import workload as W
+
+    s = W.uneven_specs()
+    assert s == W.uneven_specs() and len(s) == 2000 and len({x[3] for x in s}) == 2000
+    ns = np.array([x[0] for x in s])
+    ps = np.array([x[1] for x in s])
+    assert ns.min() >= 60 and ns.max() <= 400 and ps.min() >= 0.1 and ps.max() <= 0.9
+    assert {x[2] for x in s} == {"pm1", "int10"}
+    for spec in s[:3]:
+        n, e, w, SL = W.uneven_instance(spec)
+        n2, e2, w2, SL2 = W.uneven_instance(spec)
+        assert n == spec[0] and np.array_equal(SL, SL2) and SL.size == n * n
+        assert set(np.unique(w)) <= ({-1.0, 1.0} if spec[2] == "pm1" else set(range(-10, 11)))
+
+
 def test_bench_reference_arm_prints_one_json_line():
     r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--workload",
                         "gnp100_one_tri", "--steps", "1", "--warmup", "0", "--cpu-sample", "2", "--no-compare"],
