@@ -12,9 +12,18 @@
  * the first call from SP (the reference keeps one problem per process). */
 #include <stdio.h>
 #include <stdlib.h>
+#include <string.h>
 
 #include "admm.h"
 #include "mcbound.h"
+
+/* The one routine of operators.c that the kept files call: readData builds the
+ * Laplacian with it (process_input.c:265-268).  X = diagonal matrix of y, n x n,
+ * column-major, all off-diagonal entries zero (operators.c:44-54). */
+void Diag(double *X, const double *y, int n) {
+    memset(X, 0, (size_t)n * n * sizeof(double));
+    for (int i = 0; i < n; ++i) X[i + (size_t)i * n] = y[i];
+}
 
 extern Parameters params;
 extern double diff;

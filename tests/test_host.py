@@ -207,6 +207,33 @@ def test_reference_shim_compiles_against_the_reference_headers():
     assert r.returncode == 0, r.stderr
 
 
+@pytest.mark.skipif(not os.path.isdir("/root/reference"), reason="reference sources not present")
+def test_reference_driver_links_against_the_library(tmp_path):
+    """The reference's own driver, heap, input and heuristic files, linked with the
+    shim in place of the bound files and with libmcbound, resolve every symbol.
+    Without a device the first Evaluate ends with the shim's message and exit 1;
+    with one, the run reaches the reference's optimum."""
+    from madam_gb300 import build as B
+    from madam_gb300 import lib as M
+    from oracle import build as OB
+
+    B.build()
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    mk = subprocess.run(["make", "-s", "-C", os.path.join(root, "oracle", "ref"), "REFDIR=/root/reference",
+                         "LAPACK=" + OB.find_lapack(), "../_ref/madam_drop_in"], capture_output=True, text=True)
+    assert mk.returncode == 0, mk.stderr[-2000:]
+    n, e, w = G.gnp(40, 0.5, "one", seed=1)  # the reference fixture gnp40_one_s1 (optimum 246)
+    G.write_rudy(str(tmp_path / "g.rudy"), n, e, w)
+    (tmp_path / "params").write_text("".join("%s = %s\n" % kv for kv in M.SHIPPED.items()))
+    r = subprocess.run([os.path.join(root, "oracle", "_ref", "madam_drop_in"), str(tmp_path / "g.rudy"),
+                        str(tmp_path / "params")], capture_output=True, text=True, timeout=300)
+    assert "Graph has 40 vertices and 397 edges." in r.stdout
+    if r.returncode == 0:
+        assert float(re.search(r"^Maximum value = (\S+)", r.stdout, re.M).group(1)) == 246.0
+    else:
+        assert r.returncode == 1 and "mcb_create: no CUDA device" in r.stderr, (r.returncode, r.stderr)
+
+
 def test_newton_schulz_schedule_against_a_restatement():
     """The library's step schedule (host arithmetic, no device) is the scaled
     Newton-Schulz iteration of Chen & Chow: k^2 = 3 (1 - 0.02) / (1 + l + l^2),
