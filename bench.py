@@ -376,6 +376,8 @@ def _tto_worker(rank, world, port, q):
         os.environ[v] = "1"
     os.environ["MASTER_ADDR"] = "127.0.0.1"
     os.environ["MASTER_PORT"] = str(port)
+    # a launcher's agent store would make every rank of this private group a store client
+    os.environ.pop("TORCHELASTIC_USE_AGENT_STORE", None)
     import torch.distributed as dist
 
     dist.init_process_group("gloo", rank=rank, world_size=world)
