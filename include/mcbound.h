@@ -41,6 +41,8 @@ enum mcb_status {
     MCB_ERR_ITER = -6,     /* a device iteration cap was reached (CG, bisection) */
     MCB_ERR_NODEV = -7     /* no CUDA device                                     */
 };
+/* A NULL context is an argument error everywhere: calls that return a status return
+ * MCB_ERR_ARG, setters do nothing, getters return 0 (counters they write are 0). */
 
 /* Projection forms (mcb_create flags, low byte) */
 #define MCB_PROJ_FP64 0x0      /* plain: FP64 tridiagonal eigensolver (dsyevr's method) */

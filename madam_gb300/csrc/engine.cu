@@ -1523,15 +1523,19 @@ void mcb_destroy(mcb_ctx *c) {
 }
 
 void mcb_set_lb(mcb_ctx *c, double lb, const int *sol) {
+    if (!c) return;
     c->LB = lb;
     if (sol) c->best_sol.assign(sol, sol + c->pb);
 }
 double mcb_get_lb(const mcb_ctx *c, int *sol) {
+    if (!c) return 0.0;
     if (sol) memcpy(sol, c->best_sol.data(), c->pb * sizeof(int));
     return c->LB;
 }
-void mcb_set_diff(mcb_ctx *c, double d) { c->diff = d; }
-double mcb_get_diff(const mcb_ctx *c) { return c->diff; }
+void mcb_set_diff(mcb_ctx *c, double d) {
+    if (c) c->diff = d;
+}
+double mcb_get_diff(const mcb_ctx *c) { return c ? c->diff : 0.0; }
 int mcb_set_models(mcb_ctx *c, mcb_mlp *scorer, mcb_mlp *warm) {
     if (!c) return MCB_ERR_ARG;
     if ((scorer && mcb_mlp_num_params(scorer) <= 0) || (warm && mcb_mlp_num_params(warm) <= 0)) return MCB_ERR_ARG;
@@ -1626,11 +1630,20 @@ int mcb_ns_schedule(const mcb_ctx *c, int cap, float *a, float *b, int *accurate
     }
     return (int)c->ns.steps.size();
 }
-void mcb_set_trials(mcb_ctx *c, int p, int h) { c->prm.Pent_Trials = p; c->prm.Hepta_Trials = h; }
-void mcb_get_trials(const mcb_ctx *c, int *p, int *h) { *p = c->prm.Pent_Trials; *h = c->prm.Hepta_Trials; }
+void mcb_set_trials(mcb_ctx *c, int p, int h) {
+    if (!c) return;
+    c->prm.Pent_Trials = p;
+    c->prm.Hepta_Trials = h;
+}
+void mcb_get_trials(const mcb_ctx *c, int *p, int *h) {
+    if (p) *p = c ? c->prm.Pent_Trials : 0;
+    if (h) *h = c ? c->prm.Hepta_Trials : 0;
+}
 
 int mcb_bound_batch(mcb_ctx *c, mcb_bab_node *const *nodes, int count, int rank, double *bounds, mcb_node_stats *stats) {
     if (!c || !nodes || count < 1) return MCB_ERR_ARG;
+    for (int i = 0; i < count; ++i)
+        if (!nodes[i]) return MCB_ERR_ARG;
     c->err.clear();
     int rc = MCB_OK;
     for (int off = 0; off < count && rc == MCB_OK; off += c->batch_max) {
@@ -1806,12 +1819,13 @@ int mcb_kernel_stats(const mcb_ctx *c, int cap, char (*names)[32], long long *la
     int k = 0;
     for (int i = 0; i < K_NCLASS && k < cap; ++i, ++k) {
         if (names) snprintf(names[k], 32, "%s", kClassNames[i]);
-        if (launches) launches[k] = c->launches[i];
-        if (ms) ms[k] = c->ms[i];
+        if (launches) launches[k] = c ? c->launches[i] : 0;
+        if (ms) ms[k] = c ? c->ms[i] : 0.0;
     }
     return k;
 }
 void mcb_reset_kernel_stats(mcb_ctx *c) {
+    if (!c) return;
     for (int i = 0; i < K_NCLASS; ++i) { c->launches[i] = 0; c->ms[i] = 0; c->work[i] = 0; }
     c->h2d = c->d2h = 0;
     c->lib_launches = 0;
@@ -1839,18 +1853,19 @@ void mcb_set_profile(mcb_ctx *c, int on) {
     }
 }
 void mcb_transfer_stats(const mcb_ctx *c, long long *h2d_bytes, long long *d2h_bytes) {
-    if (h2d_bytes) *h2d_bytes = c->h2d;
-    if (d2h_bytes) *d2h_bytes = c->d2h;
+    if (h2d_bytes) *h2d_bytes = c ? c->h2d : 0;
+    if (d2h_bytes) *d2h_bytes = c ? c->d2h : 0;
 }
 int mcb_kernel_work(const mcb_ctx *c, int cap, double *work, int *unit) {
     int k = 0;
     for (int i = 0; i < K_NCLASS && k < cap; ++i, ++k) {
-        if (work) work[k] = c->work[i];
+        if (work) work[k] = c ? c->work[i] : 0.0;
         if (unit) unit[k] = kWorkUnit[i];
     }
     return k;
 }
 long long mcb_launch_count(const mcb_ctx *c) {
+    if (!c) return 0;
     long long t = 0;
     for (int i = 0; i < K_NCLASS; ++i) t += c->launches[i];
     return t;

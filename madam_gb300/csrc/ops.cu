@@ -141,6 +141,7 @@ extern "C" {
 int mcb_op_B(int n, const double *X, int ntri, const int *tri, int npent, const int *pent, int nhept, const int *hept,
              double *y) {
     if (n < 1 || n > MCB_NMAX || !X || !y || ntri < 0 || npent < 0 || nhept < 0) return MCB_ERR_ARG;
+    if ((ntri && !tri) || (npent && !pent) || (nhept && !hept)) return MCB_ERR_ARG;
     if (int rc = check_dev()) return rc;
     CutLists cl = make_lists(ntri, tri, npent, pent, nhept, hept);
     if (!valid_cuts(n, cl)) return MCB_ERR_ARG;
@@ -161,6 +162,7 @@ int mcb_op_B(int n, const double *X, int ntri, const int *tri, int npent, const 
 int mcb_op_Bt(int n, double *X, int ntri, const int *tri, int npent, const int *pent, int nhept, const int *hept,
               const double *t) {
     if (n < 1 || n > MCB_NMAX || !X || !t || ntri < 0 || npent < 0 || nhept < 0) return MCB_ERR_ARG;
+    if ((ntri && !tri) || (npent && !pent) || (nhept && !hept)) return MCB_ERR_ARG;
     if (int rc = check_dev()) return rc;
     CutLists cl = make_lists(ntri, tri, npent, pent, nhept, hept);
     if (!valid_cuts(n, cl)) return MCB_ERR_ARG;

@@ -59,6 +59,58 @@ def test_library_loads_without_a_device():
     assert L.mcb_strerror(-5) == b"capacity exceeded"
 
 
+def test_context_entry_points_accept_a_null_context():
+    """Status codes, never a crash: every entry point that takes a context treats
+    NULL as an argument error (setters do nothing, getters return 0)."""
+    import ctypes as C
+
+    from madam_gb300 import build as B
+
+    L = C.CDLL(B.build())
+    L.mcb_get_lb.restype = C.c_double
+    L.mcb_get_diff.restype = C.c_double
+    L.mcb_launch_count.restype = C.c_longlong
+    L.mcb_library_launch_count.restype = C.c_longlong
+    L.mcb_last_error.restype = C.c_char_p
+    L.mcb_set_lb.argtypes = [C.c_void_p, C.c_double, C.c_void_p]
+    L.mcb_set_diff.argtypes = [C.c_void_p, C.c_double]
+    ERR_ARG = -1
+    L.mcb_set_lb(None, 3.0, None)
+    L.mcb_set_diff(None, 1.0)
+    L.mcb_set_trials(None, 1, 2)
+    L.mcb_reset_kernel_stats(None)
+    L.mcb_destroy(None)
+    assert L.mcb_get_lb(None, None) == 0.0 and L.mcb_get_diff(None) == 0.0
+    p, h = C.c_int(7), C.c_int(7)
+    L.mcb_get_trials(None, C.byref(p), C.byref(h))
+    L.mcb_get_trials(None, None, None)
+    assert p.value == 0 and h.value == 0
+    a, b = C.c_longlong(5), C.c_longlong(5)
+    L.mcb_transfer_stats(None, C.byref(a), C.byref(b))
+    assert a.value == 0 and b.value == 0
+    assert L.mcb_launch_count(None) == 0 and L.mcb_library_launch_count(None) == 0
+    launches, ms = (C.c_longlong * 64)(), (C.c_double * 64)()
+    k = L.mcb_kernel_stats(None, 64, None, launches, ms)
+    assert k > 0 and all(launches[i] == 0 and ms[i] == 0.0 for i in range(k))
+    work, unit = (C.c_double * 64)(), (C.c_int * 64)()
+    assert L.mcb_kernel_work(None, 64, work, unit) == k
+    assert L.mcb_last_error(None) == b""
+    node = C.create_string_buffer(4 * 1024 * 2 + 8 * 1024 + 16)
+    bound = C.c_double()
+    assert L.mcb_evaluate(None, node, 1, C.byref(bound), None) == ERR_ARG
+    assert L.mcb_bound_batch(None, None, 1, 1, None, None) == ERR_ARG
+    assert L.mcb_bab(None, 1, 0, None, None, None, None, None, 0, None) == ERR_ARG
+    assert L.mcb_set_models(None, None, None) == ERR_ARG
+    assert L.mcb_log_count(None, 0) == 0 and L.mcb_log_fetch(None, 0, 0, None, None) == ERR_ARG
+    assert L.mcb_autotune_table(None, 0, None, None, None, None, None) == 0
+    # operator entry points check their arrays before they look for a device
+    X, y = (C.c_double * 16)(), (C.c_double * 4)()
+    tri = (C.c_int * 4)(2, 1, 0, 1)  # (i, j, k, type), i > j > k
+    assert L.mcb_op_B(4, X, 1, None, 0, None, 0, None, y) == ERR_ARG
+    assert L.mcb_op_Bt(4, X, 0, None, 1, None, 0, None, y) == ERR_ARG
+    assert L.mcb_op_B(4, X, 1, tri, 0, None, 0, None, y) in (-7, 0)  # arguments fine: MCB_ERR_NODEV, or runs
+
+
 def test_params_and_node_layout_match_the_reference():
     from madam_gb300 import lib as M
 
