@@ -18,7 +18,10 @@ reference's master handing idle workers new subproblems (bab_functions.c:297-325
 
 `ctx` is any object with evaluate(node, rank) -> (bound, stats), set_lb(lb, sol),
 lb() -> (lb, sol) and an `N` attribute; `new_node(fixed)` builds a node with
-xfixed / sol / fracsol arrays (the BabNode layout).
+xfixed / sol / fracsol arrays (the BabNode layout).  With batch > 1 and a context
+that has bound_batch(nodes, rank) -> (bounds, stats) (the GPU library's), each rank
+pops up to `batch` open nodes per round and bounds them in one call, as the
+library's own driver does (pop-k / push-2k around mcb_bound_batch).
 """
 import heapq
 import itertools
@@ -62,7 +65,7 @@ def balance_plan(sizes):
     return plan
 
 
-def sharded_bab(ctx, new_node, dist=None, depth=2, max_nodes=100000, balance=True, info=None):
+def sharded_bab(ctx, new_node, dist=None, depth=2, max_nodes=100000, balance=True, info=None, batch=1):
     """Returns (optimum, solution vector, nodes evaluated on this rank, evaluated on all ranks).
     info (a dict, optional) receives the number of rebalancing transfers and nodes moved."""
     rank = dist.get_rank() if dist else 0
@@ -142,16 +145,26 @@ def sharded_bab(ctx, new_node, dist=None, depth=2, max_nodes=100000, balance=Tru
                             heapq.heappush(heap, (-b, next(tie), fx, new_node(fx)))
                 transfers += len(plan)
                 moved += sum(k for _, _, k in plan)
-        if heap:
+        # pop up to `batch` nodes that the incumbent does not prune (heap.c:104-168)
+        take = []
+        while heap and len(take) < batch:
             negb, _, fx, nd = heapq.heappop(heap)
             if lb + 1.0 < -negb:
-                b, _ = ctx.evaluate(nd, 1)
-                local += 1
-                lb2, sol2 = ctx.lb()
-                if lb2 > lb:
-                    lb, sol = lb2, sol2
+                take.append((fx, nd))
+        if take:
+            if len(take) > 1 and hasattr(ctx, "bound_batch"):
+                bounds, _ = ctx.bound_batch([nd for _, nd in take], 1)
+            else:
+                bounds = [ctx.evaluate(nd, 1)[0] for _, nd in take]
+            local += len(take)
+            lb2, sol2 = ctx.lb()
+            if lb2 > lb:
+                lb, sol = lb2, sol2
+            for (fx, nd), b in zip(take, bounds):
                 if lb + 1.0 < b:
                     ic = _branch_var(nd, pb)
+                    if ic < 0:  # every variable fixed: the node is a single cut, nothing to branch
+                        continue
                     for v in (0, 1):
                         f2 = dict(fx)
                         f2[ic] = v

@@ -162,7 +162,29 @@ def test_bench_reference_arm_prints_one_json_line():
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["cpu_baseline"]["kind"] == "port"
 
 
-def _sharded_worker(rank, world, port, q, depth=2):
+class _BatchedOracle:
+    """The oracle context with the GPU library's bound_batch entry point (one
+    evaluate per node), recording the batch sizes the driver asks for."""
+
+    def __init__(self, c):
+        self.c, self.N, self.sizes = c, c.N, []
+
+    def evaluate(self, nd, rank=1):
+        return self.c.evaluate(nd, rank)
+
+    def bound_batch(self, nodes, rank=1):
+        self.sizes.append(len(nodes))
+        out = [self.c.evaluate(nd, rank) for nd in nodes]
+        return [b for b, _ in out], [st for _, st in out]
+
+    def set_lb(self, lb, sol=None):
+        self.c.set_lb(lb, sol)
+
+    def lb(self):
+        return self.c.lb()
+
+
+def _sharded_worker(rank, world, port, q, depth=2, batch=1):
     import torch.distributed as dist
 
     os.environ["MASTER_ADDR"] = "127.0.0.1"
@@ -176,22 +198,28 @@ def _sharded_worker(rank, world, port, q, depth=2):
     n, e, w = G2.gnp(64, 0.5, "pm1", seed=13)
     SL = O.build_L(n, (e, w))
     ctx = O.Ctx(O.shipped_params(), SL, n)
+    if batch > 1:
+        ctx = _BatchedOracle(ctx)
     info = {}
-    best, sol, mine, total = sharded_bab(ctx, lambda fx: O.make_node(n - 1, fx), dist=dist, depth=depth, info=info)
+    best, sol, mine, total = sharded_bab(ctx, lambda fx: O.make_node(n - 1, fx), dist=dist, depth=depth, info=info,
+                                         batch=batch)
+    if batch > 1:
+        info["batch_sizes"] = ctx.sizes
     q.put((rank, best, mine, total, None if sol is None else G2.cut_value(n, e, w, sol), info))
     dist.destroy_process_group()
 
 
-@pytest.mark.parametrize("world,depth", [(2, 2), (3, 1)])
-def test_sharded_branch_and_bound_on_gloo_ranks(orc, world, depth):
+@pytest.mark.parametrize("world,depth,batch", [(2, 2, 1), (3, 1, 1), (2, 2, 4)])
+def test_sharded_branch_and_bound_on_gloo_ranks(orc, world, depth, batch):
     """Ranks expand the top of the tree, deal the frontier, rebalance when a queue
-    runs dry, and agree on the serial optimum."""
+    runs dry, and agree on the serial optimum; with batch > 1 each rank bounds
+    several open nodes per round through bound_batch."""
     import torch.multiprocessing as mp
 
     ctx = mp.get_context("spawn")
     q = ctx.Queue()
-    port = 29500 + (os.getpid() + 7 * world) % 1000
-    ps = [ctx.Process(target=_sharded_worker, args=(r, world, port, q, depth)) for r in range(world)]
+    port = 29500 + (os.getpid() + 7 * world + 13 * batch) % 1000
+    ps = [ctx.Process(target=_sharded_worker, args=(r, world, port, q, depth, batch)) for r in range(world)]
     for p in ps:
         p.start()
     res = [q.get(timeout=600) for _ in ps]
@@ -208,6 +236,9 @@ def test_sharded_branch_and_bound_on_gloo_ranks(orc, world, depth):
     assert len({r[3] for r in res}) == 1
     if world == 3:  # one of three ranks starts with an empty queue (a frontier of two nodes)
         assert res[0][5]["transfers"] >= 1 and res[0][5]["moved"] >= 1
+    if batch > 1:
+        sizes = [k for r in res for k in r[5]["batch_sizes"]]
+        assert sizes and max(sizes) <= batch and max(sizes) > 1
 
 
 def test_balance_plan():
