@@ -241,6 +241,31 @@ def test_sharded_branch_and_bound_on_gloo_ranks(orc, world, depth, batch):
         assert sizes and max(sizes) <= batch and max(sizes) > 1
 
 
+def test_balance_plan_properties():
+    """On random queue sizes: receivers were empty, donors held nodes and keep at
+    least one, nobody receives twice, nodes are conserved, and an empty rank is
+    left out only when no queue could give (every remaining donor holds < 2)."""
+    from madam_gb300.sharded import balance_plan
+
+    rng = np.random.default_rng(11)
+    for _ in range(2000):
+        world = int(rng.integers(1, 9))
+        sizes = [int(v) for v in rng.integers(0, 6, size=world) * (rng.random(world) < 0.6)]
+        plan = balance_plan(sizes)
+        assert plan == balance_plan(list(sizes))  # a function of the sizes only
+        after = list(sizes)
+        receivers = [r for _, r, _ in plan]
+        assert len(receivers) == len(set(receivers))
+        for d, r, k in plan:
+            assert sizes[r] == 0 and sizes[d] > 0 and k >= 1
+            after[d] -= k
+            after[r] += k
+        assert sum(after) == sum(sizes) and all(after[d] >= 1 for d, _, _ in plan)
+        empty_left = [r for r in range(world) if after[r] == 0]
+        if empty_left:
+            assert all(after[d] < 2 for d in range(world) if sizes[d] > 0)
+
+
 def test_balance_plan():
     from madam_gb300.sharded import balance_plan
 
