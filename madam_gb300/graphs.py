@@ -22,6 +22,8 @@ def read_rudy(path):
     with open(path) as f:
         toks = f.read().split()
     n, m = int(toks[0]), int(toks[1])
+    if n <= 0:  # process_input.c:199
+        raise ValueError("number of vertices has to be positive")
     a = np.array(toks[2:2 + 3 * m], dtype=np.float64).reshape(m, 3)
     e = a[:, :2].astype(np.int32)
     if m and (e.min() < 1 or e.max() > n):
@@ -39,9 +41,16 @@ def write_rudy(path, n, edges, w):
 def extended_laplacian(n, edges, w):
     """SP->L of process_input.c:255-299 as an (n, n) array (symmetric)."""
     A = np.zeros((n, n))
-    e = np.asarray(edges, dtype=np.int64) - 1
-    A[e[:, 0], e[:, 1]] = w
-    A[e[:, 1], e[:, 0]] = w
+    e = np.asarray(edges, dtype=np.int64).reshape(-1, 2) - 1
+    w = np.asarray(w, dtype=np.float64)
+    if len(w):
+        # readData assigns edge by edge (process_input.c:215-224): a pair listed
+        # twice, in either orientation, keeps its last weight on both sides
+        lo, hi = np.minimum(e[:, 0], e[:, 1]), np.maximum(e[:, 0], e[:, 1])
+        _, last = np.unique((lo * n + hi)[::-1], return_index=True)
+        keep = len(w) - 1 - last
+        A[lo[keep], hi[keep]] = w[keep]
+        A[hi[keep], lo[keep]] = w[keep]
     deg = A.sum(axis=1)
     m = n - 1
     L = np.zeros((n, n))

@@ -22,6 +22,29 @@ def test_extended_laplacian_matches_oracle(orc):
         assert np.array_equal(G.extended_laplacian(n, e, w).ravel(order="F"), orc.build_L(n, (e, w)))
 
 
+def test_repeated_edges_and_self_loops_follow_the_reference(orc, tmp_path):
+    """readData assigns weights edge by edge: a pair listed twice, in either
+    orientation, keeps its last weight on both sides, and a self-loop cancels in
+    the Laplacian.  A non-positive vertex count is an input error."""
+    n = 5
+    e = np.array([[1, 2], [2, 1], [3, 3], [4, 5], [4, 5], [1, 5]], dtype=np.int32)
+    w = np.array([1.0, 7.0, 3.0, 2.0, -4.0, 1.0])
+    L = G.extended_laplacian(n, e, w)
+    assert np.array_equal(L.ravel(order="F"), orc.build_L(n, (e, w)))
+    assert np.array_equal(L, L.T) and L[0, 1] == -7.0 and L[3, 3] == -4.0  # edge (4, 5): last weight -4
+    rng = np.random.default_rng(3)
+    for _ in range(20):
+        n = int(rng.integers(3, 30))
+        m = int(rng.integers(1, 3 * n))
+        e = rng.integers(1, n + 1, size=(m, 2)).astype(np.int32)
+        w = rng.integers(-5, 6, size=m).astype(np.float64)
+        assert np.array_equal(G.extended_laplacian(n, e, w).ravel(order="F"), orc.build_L(n, (e, w)))
+    f = tmp_path / "bad.rudy"
+    f.write_text("0 1\n1 1 1\n")
+    with pytest.raises(ValueError):
+        G.read_rudy(str(f))
+
+
 def test_rudy_roundtrip(tmp_path):
     n, e, w = G.gnp(20, 0.5, "int10", seed=4)
     f = tmp_path / "g.rudy"
