@@ -36,7 +36,7 @@ def collect(instances, proj=M.PROJ_FP64, batch=8, max_nodes=400, params=None):
         try:
             ctx.bab(batch=batch, max_nodes=max_nodes)
         except M.MCBError:
-            pass  # node limit: keep what was logged
+            pass  # a failed run keeps what was logged (a node limit returns normally)
         a, b = ctx.log(M.LOG_SCORER)
         c, d = ctx.log(M.LOG_WARM)
         xs.append(a); ys.append(b); xw.append(c); yw.append(d)

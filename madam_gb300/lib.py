@@ -241,9 +241,13 @@ class Context:
         log = (NodeStats * log_cap)()
         rc = lib().mcb_bab(self.h, batch, max_nodes, C.byref(opt), sol.ctypes.data, C.byref(rb), C.byref(nodes),
                            C.cast(log, C.c_void_p), log_cap, C.byref(lc))
-        _check(rc, self.h)
+        # the node limit ends the search early with the incumbent so far, as the
+        # reference's time limit does (bab_functions.c:360-369): not an error
+        stopped = rc == ERR_CAPACITY and max_nodes > 0 and lib().mcb_last_error(self.h) == b"node limit reached"
+        if not stopped:
+            _check(rc, self.h)
         return dict(nodes=nodes.value, opt=opt.value, sol=sol[: self.N - 1].copy(), root_bound=rb.value,
-                    log=[log[i] for i in range(lc.value)])
+                    log=[log[i] for i in range(lc.value)], stopped=stopped)
 
     def kernel_stats(self):
         cap = 64

@@ -7,7 +7,7 @@ report of bab_functions.c (printFinalOutput / printSolution, :340-373), so a run
 can be diffed against the reference's .output files.  The branch-and-bound is
 the library's batched driver (mcb_bab) on the GPU.
 
-    python -m madam_gb300.solve INSTANCE PARAMS [--form learned|mixed|fp64] [--batch 64] [--out FILE]
+    python -m madam_gb300.solve INSTANCE PARAMS [--form learned|mixed|fp64] [--batch 64] [--max-nodes K] [--out FILE]
 """
 import argparse
 import os
@@ -56,15 +56,18 @@ def format_params(vals):
 
 
 def report(instance, n, n_edges, vals, result, seconds):
-    """The reference's output file text for one finished run."""
+    """The reference's output file text for one run (printFinalOutput,
+    bab_functions.c:353-373; a run stopped by its node limit is reported as the
+    reference reports one stopped by its time limit)."""
     sol = " ".join(str(i + 1) for i, x in enumerate(result["sol"]) if x == 1)
     return "".join([
         "Input file: %s\n" % instance,
         "\nGraph has %d vertices and %d edges.\n" % (n, n_edges),
         format_params(vals) + "\n",
         "\nNodes = %d\n" % result["nodes"],
+        "TIME LIMIT REACHED.\n" if result.get("stopped") else "",
         "Root node bound = %.2f\n" % result["root_bound"],
-        "Maximum value = %.0f\n" % result["opt"],
+        ("Best value = %.0f\n" if result.get("stopped") else "Maximum value = %.0f\n") % result["opt"],
         "Solution = ( %s%s)\n" % (sol, " " if sol else ""),
         "Time = %.2f s\n\n" % seconds,
     ])
@@ -96,9 +99,10 @@ def main(argv=None):
     ap.add_argument("params")
     ap.add_argument("--form", default="mixed", choices=["learned", "mixed", "fp64"])
     ap.add_argument("--batch", type=int, default=64)
+    ap.add_argument("--max-nodes", type=int, default=0, help="stop after this many node bounds (0: none)")
     ap.add_argument("--out", default=None, help="report file (default: INSTANCE.output)")
     a = ap.parse_args(argv)
-    text, _ = solve(a.instance, a.params, a.form, a.batch)
+    text, _ = solve(a.instance, a.params, a.form, a.batch, a.max_nodes)
     sys.stdout.write(text)
     with open(a.out or a.instance + ".output", "w") as f:
         f.write(text)

@@ -324,6 +324,12 @@ def test_solve_reads_parameter_files(tmp_path):
     assert re.search(r"sigma0 = (\S+)", txt).group(1) == "1.600000"
     assert re.search(r"^Time = (\S+) s", txt, re.M).group(1) == "12.35"
     assert "Graph has 6 vertices and 9 edges." in txt
+    assert "TIME LIMIT REACHED." not in txt and "Best value" not in txt
+    # a run stopped by its node limit reads like the reference's early stop
+    stop = S.report("g.rudy", 6, 9, v, dict(res, stopped=True), 1.0)
+    tail = stop[stop.index("\nNodes = "):].splitlines()
+    assert tail[1:5] == ["Nodes = 41", "TIME LIMIT REACHED.", "Root node bound = 1447.82", "Best value = 1435"]
+    assert "Maximum value" not in stop
 
 
 @pytest.mark.skipif(not os.path.isdir("/root/reference"), reason="reference headers not present")
