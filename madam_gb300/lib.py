@@ -38,6 +38,14 @@ PARAM_FIELDS = [
     ("use_diff", C.c_int), ("branchingStrategy", C.c_int),
 ]
 
+# the reference's compiled-in defaults (PARAM_FIELDS, admm.h:59-81): what a name
+# missing from a parameter file keeps
+COMPILED_DEFAULTS = dict(sigma0=1.0, scaleSigma=1.001, ADMM_itermax=2000, tol0=5e-2, scaleTol=0.6, minTol=1e-4,
+                         triag_iter=5, pent_iter=5, hept_iter=5, max_outer_iter=20, extra_iter=10,
+                         violated_TriIneq=1e-3, TriIneq=5000, adjust_TriIneq=1, PentIneq=5000, HeptaIneq=5000,
+                         Pent_Trials=60, Hepta_Trials=50, include_Pent=1, include_Hepta=1, root=0, use_diff=1,
+                         branchingStrategy=1)
+
 # defaults of the reference's shipped parameter file (params:1-23)
 SHIPPED = dict(sigma0=1.0, scaleSigma=1.001, ADMM_itermax=2000, tol0=5e-2, scaleTol=0.6, minTol=1e-3,
                triag_iter=3, pent_iter=3, hept_iter=3, max_outer_iter=12, extra_iter=5,

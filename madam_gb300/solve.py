@@ -1,16 +1,17 @@
 """Command-line branch-and-bound in the reference's formats.
 
 Reads a rudy-format instance and a parameter file the way process_input.c does
-(readParameters, process_input.c:141-178: "name = value" lines, unknown names
-ignored, missing ones at their defaults; readData, :182-312) and writes the
-report of bab_functions.c (printFinalOutput / printSolution, :340-373), so a run
-can be diffed against the reference's .output files.  The branch-and-bound is
-the library's batched driver (mcb_bab) on the GPU.
+(readParameters, process_input.c:141-178, with its line semantics restated in
+read_params; readData, :182-312) and writes the report of bab_functions.c
+(printFinalOutput / printSolution, :337-373), so a run can be diffed against the
+reference's .output files.  The branch-and-bound is the library's batched driver
+(mcb_bab) on the GPU.
 
     python -m madam_gb300.solve INSTANCE PARAMS [--form learned|mixed|fp64] [--batch 64] [--max-nodes K] [--out FILE]
 """
 import argparse
 import os
+import re
 import sys
 import time
 
@@ -26,24 +27,60 @@ _FLOAT = {"sigma0", "scaleSigma", "tol0", "scaleTol", "minTol", "violated_TriIne
 PARAM_ORDER = [name for name, _ in M.PARAM_FIELDS]
 
 
+_NAME = re.compile(r"[^=^ ]+")
+_INT = re.compile(r"[ \t\n\v\f\r]*([+-]?[0-9]+)")
+_DEC = re.compile(r"[ \t\n\v\f\r]*([+-]?(?:[0-9]+\.?[0-9]*|\.[0-9]+)(?:[eE][+-]?[0-9]+)?)")
+_HEX = re.compile(r"[ \t\n\v\f\r]*([+-]?0[xX](?:[0-9a-fA-F]+\.?[0-9a-fA-F]*|\.[0-9a-fA-F]+)(?:[pP][+-]?[0-9]+)?)")
+_SPECIAL = re.compile(r"[ \t\n\v\f\r]*([+-]?(?:inf(?:inity)?|nan))", re.I)
+
+
+def _scan_int(s):
+    """C's %d: leading white space, a sign, at least one digit; None if no number."""
+    m = _INT.match(s)
+    return int(m.group(1)) if m else None
+
+
+def _scan_double(s):
+    """C's %lf (strtod): the longest numeric prefix; None if no number."""
+    for rx, conv in ((_HEX, float.fromhex), (_SPECIAL, float), (_DEC, float)):
+        m = rx.match(s)
+        if m:
+            return conv(m.group(1))
+    return None
+
+
+def _pieces(text):
+    """What fgets(s, 120, f) returns, one call at a time: at most 119 characters,
+    ending after a newline; C sees each up to its first NUL."""
+    for line in re.findall(r"[^\n]*\n|[^\n]+$", text):
+        for k in range(0, len(line), 119):
+            yield line[k:k + 119].split("\0")[0]
+
+
 def read_params(path):
-    """Parameter file -> dict over every field (defaults = the shipped file's values)."""
-    vals = dict(M.SHIPPED)
-    with open(path) as f:
-        for line in f:
-            if "=" not in line:
-                continue
-            name, _, rest = line.partition("=")
-            name = name.strip()
-            if name not in vals:
-                continue
-            tok = rest.split()
-            if not tok:
-                continue
-            try:
-                vals[name] = float(tok[0]) if name in _FLOAT else int(float(tok[0]))
-            except ValueError:
-                pass
+    """Parameter file -> dict over every field, as readParameters reads it
+    (process_input.c:141-178).  Names missing from the file keep the compiled-in
+    defaults (admm.h:59-81).  Per fgets piece: the name is the longest prefix of
+    characters other than '=', '^' and ' '; a piece that starts with one of those
+    keeps the previous piece's name.  If that name is a parameter, the value is the
+    number (C's %d or %lf) after the first '=', which needs at least one character
+    before it; a piece without one changes nothing."""
+    vals = dict(M.COMPILED_DEFAULTS)
+    with open(path, "rb") as f:
+        text = f.read().decode("latin-1")
+    name = None
+    for piece in _pieces(text):
+        m = _NAME.match(piece)
+        if m:
+            name = m.group(0)
+        if name not in vals:
+            continue
+        eq = piece.find("=")
+        if eq < 1:
+            continue
+        v = (_scan_double if name in _FLOAT else _scan_int)(piece[eq + 1:])
+        if v is not None:
+            vals[name] = v
     return vals
 
 

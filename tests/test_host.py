@@ -300,6 +300,39 @@ def test_balance_plan():
 
 
 # ---- reference-format command line (madam_gb300/solve.py) ----------------------
+REF_SO = os.path.join(ROOT, "oracle", "_ref", "libmadam_ref_strict.so")
+
+
+@pytest.mark.skipif(not os.path.exists(REF_SO), reason="reference build (oracle/_ref) not present")
+def test_parameter_files_read_like_the_reference(tmp_path):
+    """read_params against the reference's own readParameters (the strict build in
+    oracle/_ref) on seeded files made of well-formed, indented, tabbed, blank,
+    over-long and malformed lines."""
+    import ctypes as C
+
+    from madam_gb300 import lib as M
+    from madam_gb300 import solve as S
+
+    R = C.CDLL(REF_SO)
+    P = M.Params.in_dll(R, "params")
+    names = [k for k, _ in M.PARAM_FIELDS]
+    values = ["1.6", "7", "-2", "1e-4", "2.5e1x", ".5", "12.7", "abc", "", "0x10", "inf", " 3 ", "+4"]
+    rng = np.random.default_rng(17)
+    for case in range(300):
+        lines = []
+        for _ in range(int(rng.integers(0, 12))):
+            nm = names[int(rng.integers(len(names)))] if rng.random() < 0.8 else "unknown"
+            val = values[int(rng.integers(len(values)))]
+            shape = int(rng.integers(0, 9))
+            lines.append([nm + " = " + val, nm + "=" + val, "  " + nm + " = " + val, nm + "\t= " + val, "",
+                          nm + " " + val, "= " + val, nm + " = " + val + " " * 130, nm + "^x = " + val][shape])
+        f = tmp_path / ("p%d" % case)
+        f.write_text("\n".join(lines) + ("\n" if rng.random() < 0.7 else ""))
+        assert R.readParameters(str(f).encode(), 0) == 0
+        ref = {k: getattr(P, k) for k in names}
+        assert S.read_params(str(f)) == ref, (lines, S.read_params(str(f)), ref)
+
+
 def test_solve_reads_parameter_files(tmp_path):
     import re
 
@@ -307,10 +340,16 @@ def test_solve_reads_parameter_files(tmp_path):
     from madam_gb300 import solve as S
 
     p = tmp_path / "params"
-    p.write_text("sigma0 = 1.6\nscaleSigma=1.002\n  unknown_name = 7\nTriIneq = 1500   \nminTol = 1e-4\n")
+    p.write_text("sigma0 = 1.6\nscaleSigma=1.002\nTriIneq = 1500   \nminTol = 1e-3\nbogus = 4\n")
     v = S.read_params(str(p))
-    assert v["sigma0"] == 1.6 and v["scaleSigma"] == 1.002 and v["TriIneq"] == 1500 and v["minTol"] == 1e-4
-    assert all(v[k] == M.SHIPPED[k] for k in M.SHIPPED if k not in ("sigma0", "scaleSigma", "TriIneq", "minTol"))
+    assert v["sigma0"] == 1.6 and v["scaleSigma"] == 1.002 and v["TriIneq"] == 1500 and v["minTol"] == 1e-3
+    # names the file leaves out keep the compiled-in defaults, not the shipped file's values
+    assert all(v[k] == M.COMPILED_DEFAULTS[k] for k in M.COMPILED_DEFAULTS
+               if k not in ("sigma0", "scaleSigma", "TriIneq", "minTol"))
+    # an indented line keeps the previous line's name (readParameters' sscanf); numbers are C prefixes
+    p.write_text("scaleSigma=1.002\n  unknown_name = 7\nTriIneq = 1e-4\nsigma0 = 1.6abc\nminTol\t= 9\n")
+    v2 = S.read_params(str(p))
+    assert v2["scaleSigma"] == 7.0 and v2["TriIneq"] == 1 and v2["sigma0"] == 1.6 and v2["minTol"] == 1e-4
     ref = "/root/reference/params"
     if os.path.exists(ref):
         assert S.read_params(ref) == {k: type(M.SHIPPED[k])(v) for k, v in M.SHIPPED.items()}
