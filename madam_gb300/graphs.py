@@ -18,17 +18,35 @@ import numpy as np
 
 
 def read_rudy(path):
-    """Return (n, edges[m,2] 1-based int32, weights[m] float64)."""
-    with open(path) as f:
-        toks = f.read().split()
-    n, m = int(toks[0]), int(toks[1])
+    """Return (n, edges[m,2] 1-based int32, weights[m] float64), reading the file as
+    readData does (process_input.c:182-224): fscanf "%d %d" for the header, then
+    "%d %d %lf" per edge over one stream of white-space separated numbers.  A
+    failed conversion, a vertex count below 1 or a vertex out of range raises
+    ValueError; a negative edge count reads no edges; text after the edges is
+    ignored."""
+    from . import cformat as C
+
+    with open(path, "rb") as f:
+        text = f.read().decode("latin-1")
+    n, pos = C.scan_int(text, 0)
+    m, pos = C.scan_int(text, pos) if n is not None else (None, pos)
+    if n is None or m is None:
+        raise ValueError("problem reading number of vertices and edges")
     if n <= 0:  # process_input.c:199
         raise ValueError("number of vertices has to be positive")
-    a = np.array(toks[2:2 + 3 * m], dtype=np.float64).reshape(m, 3)
-    e = a[:, :2].astype(np.int32)
-    if m and (e.min() < 1 or e.max() > n):
-        raise ValueError("vertex out of range")
-    return n, e, a[:, 2].copy()
+    e = np.zeros((max(m, 0), 2), dtype=np.int32)
+    w = np.zeros(max(m, 0))
+    for k in range(max(m, 0)):
+        i, pos = C.scan_int(text, pos)
+        j, pos = C.scan_int(text, pos) if i is not None else (None, pos)
+        x, pos = C.scan_double(text, pos) if j is not None else (None, pos)
+        if x is None:
+            raise ValueError("problem reading edges of the graph")
+        if not (1 <= i <= n and 1 <= j <= n):
+            raise ValueError("problem with edge: vertex not in range")
+        e[k] = (i, j)
+        w[k] = x
+    return n, e, w
 
 
 def write_rudy(path, n, edges, w):
@@ -51,16 +69,18 @@ def extended_laplacian(n, edges, w):
         keep = len(w) - 1 - last
         A[lo[keep], hi[keep]] = w[keep]
         A[hi[keep], lo[keep]] = w[keep]
-    deg = A.sum(axis=1)
+    # every sum in the reference's order (process_input.c:255-299), left to right;
+    # np.cumsum accumulates strictly in sequence, unlike np.sum's pairwise tree
+    deg = np.cumsum(A, axis=0)[-1]
     m = n - 1
     L = np.zeros((n, n))
     Lap = np.diag(deg[:m]) - A[:m, :m]
     L[:m, :m] = Lap
-    # vector part: row sums of Lap taken in the reference's accumulation order
-    rs = np.array([sum(Lap[ii, jj] for jj in range(m)) for ii in range(m)]) if m <= 64 else Lap.sum(axis=1)
-    L[:m, m] = rs
-    L[m, :m] = rs
-    L[m, m] = rs.sum()
+    if m > 0:
+        rs = np.cumsum(Lap, axis=0)[-1]  # column sums of Lap, top to bottom
+        L[:m, m] = rs
+        L[m, :m] = rs
+        L[m, m] = np.cumsum(rs)[-1]
     return L
 
 

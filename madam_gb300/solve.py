@@ -19,6 +19,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 if os.path.dirname(HERE) not in sys.path:
     sys.path.insert(0, os.path.dirname(HERE))
 
+from madam_gb300 import cformat as C  # noqa: E402
 from madam_gb300 import graphs as G  # noqa: E402
 from madam_gb300 import lib as M  # noqa: E402
 
@@ -28,25 +29,6 @@ PARAM_ORDER = [name for name, _ in M.PARAM_FIELDS]
 
 
 _NAME = re.compile(r"[^=^ ]+")
-_INT = re.compile(r"[ \t\n\v\f\r]*([+-]?[0-9]+)")
-_DEC = re.compile(r"[ \t\n\v\f\r]*([+-]?(?:[0-9]+\.?[0-9]*|\.[0-9]+)(?:[eE][+-]?[0-9]+)?)")
-_HEX = re.compile(r"[ \t\n\v\f\r]*([+-]?0[xX](?:[0-9a-fA-F]+\.?[0-9a-fA-F]*|\.[0-9a-fA-F]+)(?:[pP][+-]?[0-9]+)?)")
-_SPECIAL = re.compile(r"[ \t\n\v\f\r]*([+-]?(?:inf(?:inity)?|nan))", re.I)
-
-
-def _scan_int(s):
-    """C's %d: leading white space, a sign, at least one digit; None if no number."""
-    m = _INT.match(s)
-    return int(m.group(1)) if m else None
-
-
-def _scan_double(s):
-    """C's %lf (strtod): the longest numeric prefix; None if no number."""
-    for rx, conv in ((_HEX, float.fromhex), (_SPECIAL, float), (_DEC, float)):
-        m = rx.match(s)
-        if m:
-            return conv(m.group(1))
-    return None
 
 
 def _pieces(text):
@@ -78,7 +60,7 @@ def read_params(path):
         eq = piece.find("=")
         if eq < 1:
             continue
-        v = (_scan_double if name in _FLOAT else _scan_int)(piece[eq + 1:])
+        v, _ = (C.scan_double if name in _FLOAT else C.scan_int)(piece, eq + 1)
         if v is not None:
             vals[name] = v
     return vals

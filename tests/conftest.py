@@ -11,6 +11,9 @@ if ROOT not in sys.path:
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA device (GB300) and the built libmcbound.so")
     config.addinivalue_line("markers", "slow: long CPU run (minutes)")
+    # temporary files of the tests stay inside the repository (git-ignored)
+    if not config.option.basetemp:
+        config.option.basetemp = os.path.join(ROOT, ".pytest_tmp")
 
 
 def has_gpu():

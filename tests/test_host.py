@@ -33,16 +33,65 @@ def test_repeated_edges_and_self_loops_follow_the_reference(orc, tmp_path):
     assert np.array_equal(L.ravel(order="F"), orc.build_L(n, (e, w)))
     assert np.array_equal(L, L.T) and L[0, 1] == -7.0 and L[3, 3] == -4.0  # edge (4, 5): last weight -4
     rng = np.random.default_rng(3)
-    for _ in range(20):
-        n = int(rng.integers(3, 30))
+    for k in range(40):  # fractional weights and n > 64 too: every sum in the reference's order
+        n = int(rng.integers(3, 30 if k < 20 else 140))
         m = int(rng.integers(1, 3 * n))
         e = rng.integers(1, n + 1, size=(m, 2)).astype(np.int32)
-        w = rng.integers(-5, 6, size=m).astype(np.float64)
+        w = rng.integers(-5, 6, size=m).astype(np.float64) if k % 2 else 3.7 * rng.standard_normal(m)
         assert np.array_equal(G.extended_laplacian(n, e, w).ravel(order="F"), orc.build_L(n, (e, w)))
     f = tmp_path / "bad.rudy"
     f.write_text("0 1\n1 1 1\n")
     with pytest.raises(ValueError):
         G.read_rudy(str(f))
+
+
+@pytest.mark.skipif(not os.path.exists(os.path.join(ROOT, "oracle", "_ref", "libmadam_ref_strict.so")),
+                    reason="reference build (oracle/_ref) not present")
+def test_rudy_files_read_like_the_reference(tmp_path):
+    """read_rudy + extended_laplacian against the reference's own readData (the
+    strict build in oracle/_ref): seeded files with mixed white space, repeated
+    and reversed edges, self-loops, fractional and exponent weights, and malformed
+    or missing numbers (both sides reject the same files)."""
+    import ctypes as C
+
+    R = C.CDLL(os.path.join(ROOT, "oracle", "_ref", "libmadam_ref_strict.so"))
+    libc = C.CDLL(None)
+    libc.fopen.restype = C.c_void_p
+    libc.fopen.argtypes = [C.c_char_p, C.c_char_p]
+    C.c_void_p.in_dll(R, "output").value = libc.fopen(os.devnull.encode(), b"w")
+
+    class Problem(C.Structure):  # admm.h:121-127
+        _fields_ = [("L", C.POINTER(C.c_double)), ("n", C.c_int), ("NIneq", C.c_int), ("NPentIneq", C.c_int),
+                    ("NHeptaIneq", C.c_int)]
+
+    SP = C.POINTER(Problem).in_dll(R, "SP")
+    rng = np.random.default_rng(29)
+    weights = ["1", "-1", "7", "2.5", "-0.125", "1e1", "+3", ".5", "3.7", "x", "1.5e-2"]
+    seps = [" ", "\t", "\n", "\r\n", "  "]
+    for case in range(150):
+        n = int(rng.integers(0, 9))
+        m = int(rng.integers(-1, 8))
+        toks = [str(n), str(m)]
+        for _ in range(max(m, 0) + int(rng.integers(-1, 2))):
+            i, j = (str(int(v)) for v in rng.integers(1, n + 2, size=2)) if n else ("1", "1")
+            if rng.random() < 0.05:
+                i = "1.5"
+            toks += [i, j, weights[int(rng.integers(len(weights)))]]
+        f = tmp_path / ("g%d.rudy" % case)
+        f.write_text("".join(t + seps[int(rng.integers(len(seps)))] for t in toks))
+        rc = R.readData(str(f).encode())
+        try:
+            nn, e, w = G.read_rudy(str(f))
+            ours = G.extended_laplacian(nn, e, w).ravel(order="F")
+        except ValueError:
+            ours = None
+        if rc != 0:
+            assert ours is None, toks
+        else:
+            k = SP.contents.n
+            ref = np.ctypeslib.as_array(SP.contents.L, shape=(k * k,)).copy()
+            assert ours is not None and np.array_equal(ours, ref), toks
+    libc.fflush(None)  # readData's printf output, inside the test's capture
 
 
 def test_rudy_roundtrip(tmp_path):
