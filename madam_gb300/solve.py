@@ -79,10 +79,13 @@ def report(instance, n, n_edges, vals, result, seconds):
     bab_functions.c:353-373; a run stopped by its node limit is reported as the
     reference reports one stopped by its time limit)."""
     sol = " ".join(str(i + 1) for i, x in enumerate(result["sol"]) if x == 1)
+    shown = dict(vals)
+    if shown["adjust_TriIneq"]:  # the block is printed after the adjustment (process_input.c:119-132)
+        shown["TriIneq"] = n * 10
     return "".join([
         "Input file: %s\n" % instance,
         "\nGraph has %d vertices and %d edges.\n" % (n, n_edges),
-        format_params(vals) + "\n",
+        format_params(shown) + "\n",
         "\nNodes = %d\n" % result["nodes"],
         "TIME LIMIT REACHED.\n" if result.get("stopped") else "",
         "Root node bound = %.2f\n" % result["root_bound"],
@@ -119,12 +122,20 @@ def main(argv=None):
     ap.add_argument("--form", default="mixed", choices=["learned", "mixed", "fp64"])
     ap.add_argument("--batch", type=int, default=64)
     ap.add_argument("--max-nodes", type=int, default=0, help="stop after this many node bounds (0: none)")
-    ap.add_argument("--out", default=None, help="report file (default: INSTANCE.output)")
+    ap.add_argument("--out", default=None, help="report file (default: INSTANCE.output, never overwritten)")
     a = ap.parse_args(argv)
     text, _ = solve(a.instance, a.params, a.form, a.batch, a.max_nodes)
     sys.stdout.write(text)
-    with open(a.out or a.instance + ".output", "w") as f:
+    with open(a.out or output_path(a.instance), "w") as f:
         f.write(text)
+
+
+def output_path(instance):
+    """INSTANCE.output, or INSTANCE.output_1, _2, ... if taken (process_input.c:52-60)."""
+    path, k = instance + ".output", 1
+    while os.path.exists(path):
+        path, k = "%s.output_%d" % (instance, k), k + 1
+    return path
 
 
 if __name__ == "__main__":

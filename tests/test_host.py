@@ -382,6 +382,44 @@ def test_parameter_files_read_like_the_reference(tmp_path):
         assert S.read_params(str(f)) == ref, (lines, S.read_params(str(f)), ref)
 
 
+@pytest.mark.skipif(not os.path.exists(REF_SO), reason="reference build (oracle/_ref) not present")
+def test_report_header_and_file_name_match_the_reference(tmp_path):
+    """The reference's processCommandLineArguments writes the .output header
+    (input file, graph size, the parameters after adjust_TriIneq) into
+    INSTANCE.output, or INSTANCE.output_1, ... when taken; solve.report and
+    solve.output_path give the same text and names."""
+    import ctypes as C
+
+    from madam_gb300 import lib as M
+    from madam_gb300 import solve as S
+
+    R = C.CDLL(REF_SO)
+    libc = C.CDLL(None)
+    libc.fclose.argtypes = [C.c_void_p]
+    out = C.c_void_p.in_dll(R, "output")
+    rng = np.random.default_rng(41)
+    names = [k for k, _ in M.PARAM_FIELDS]
+    for case in range(12):
+        n, e, w = G.gnp(int(rng.integers(3, 40)), 0.4, "int10", seed=case)
+        inst = str(tmp_path / ("g%d.rudy" % case))
+        G.write_rudy(inst, n, e, w)
+        prm = tmp_path / ("p%d" % case)
+        keep = [k for k in names if rng.random() < 0.6]
+        prm.write_text("".join("%s = %s\n" % (k, M.SHIPPED[k] if rng.random() < 0.7 else M.COMPILED_DEFAULTS[k])
+                               for k in keep) + ("adjust_TriIneq = 0\n" if case % 3 == 0 else ""))
+        for run in range(2 if case == 0 else 1):
+            expect = S.output_path(inst)
+            argv = (C.c_char_p * 3)(b"biqbin", inst.encode(), str(prm).encode())
+            assert R.processCommandLineArguments(3, argv, 0) == 0
+            libc.fclose(out.value)
+            out.value = None
+            assert os.path.exists(expect) and expect.endswith(".output" if run == 0 else ".output_1")
+            ref = open(expect).read()
+            res = dict(nodes=1, root_bound=0.0, opt=0.0, sol=[])
+            ours = S.report(inst, n, len(w), S.read_params(str(prm)), res, 0.0)
+            assert ours[: ours.index("\nNodes = ")] == ref, (ours, ref)
+
+
 def test_solve_reads_parameter_files(tmp_path):
     import re
 
