@@ -418,6 +418,7 @@ def test_report_header_and_file_name_match_the_reference(tmp_path):
             res = dict(nodes=1, root_bound=0.0, opt=0.0, sol=[])
             ours = S.report(inst, n, len(w), S.read_params(str(prm)), res, 0.0)
             assert ours[: ours.index("\nNodes = ")] == ref, (ours, ref)
+    libc.fflush(None)  # readData's printf output, inside the test's capture
 
 
 def test_solve_reads_parameter_files(tmp_path):
