@@ -5,7 +5,11 @@ strict-IEEE build, oracle/_ref/madam_ref_strict) on seeded synthetic rudy-style
 instances and records, per instance, every evaluated node's bound, the node
 count, the optimum and the optimal cut vector.  The instances are regenerated
 from their seeds by madam_gb300.graphs, so the fixtures travel without the
-reference.  Run where the reference sources are present:
+reference.  reference_bab.json holds trees under the shipped parameter file;
+reference_bab_params.json holds trees under other settings (triangles only, no
+heptagons, least-fractional branching, no diff give-up, another sigma0, a fixed
+triangle budget), which exercise the remaining branches of the bound and the
+driver.  Run where the reference sources are present:
 
     python tests/golden/make_golden.py
 """
@@ -29,6 +33,15 @@ INSTANCES = [
     ("gnp64_pm1_s13", "gnp", (64, 0.5, "pm1", 13)),
     ("gnp70_one_s11", "gnp", (70, 0.5, "one", 11)),
     ("torus7x7_s15", "torus", (7, 7, 15)),
+]
+
+# (name, generator, args, parameter overrides of the shipped file)
+VARIANTS = [
+    ("gnp56_pm1_s31_tri", "gnp", (56, 0.5, "pm1", 31), dict(include_Pent=0, include_Hepta=0)),
+    ("gnp56_pm1_s39_least", "gnp", (56, 0.5, "pm1", 39), dict(branchingStrategy=0)),
+    ("gnp56_pm1_s49_nodiff", "gnp", (56, 0.5, "pm1", 49), dict(use_diff=0, sigma0=1.6)),
+    ("gnp56_pm1_s37_nohept", "gnp", (56, 0.5, "pm1", 37), dict(include_Hepta=0)),
+    ("gnp60_int10_s25_sparse", "gnp", (60, 0.2, "int10", 25), dict(TriIneq=300, adjust_TriIneq=0)),
 ]
 
 SHIPPED = """sigma0 = 1
@@ -63,12 +76,21 @@ def make_instance(kind, args):
     return G.torus2d(args[0], args[1], seed=args[2])
 
 
-def run_reference(binary, n, e, w, max_nodes=2000):
-    with tempfile.TemporaryDirectory() as d:
+def params_text(over=None):
+    """The shipped parameter file with some values replaced."""
+    lines = []
+    for line in SHIPPED.splitlines():
+        name = line.split("=")[0].strip()
+        lines.append("%s = %s" % (name, over[name]) if over and name in over else line)
+    return "\n".join(lines) + "\n"
+
+
+def run_reference(binary, n, e, w, max_nodes=2000, over=None):
+    with tempfile.TemporaryDirectory(dir=HERE) as d:
         g = os.path.join(d, "graph")
         G.write_rudy(g, n, e, w)
         p = os.path.join(d, "params")
-        open(p, "w").write(SHIPPED)
+        open(p, "w").write(params_text(over))
         out = subprocess.run([binary, g, p, str(max_nodes)], capture_output=True, text=True, cwd=d, timeout=3600)
     if out.returncode != 0:
         raise RuntimeError(out.stderr)
@@ -93,6 +115,15 @@ def main():
         print(name, "nodes", r["nodes"], "opt", r["opt"], "root %.9f" % r["bounds"][0], "evaluated", len(r["bounds"]))
     json.dump({"generator": "tests/golden/make_golden.py", "reference_build": "oracle/ref/Makefile strict flavour",
                "instances": fixtures}, open(os.path.join(HERE, "reference_bab.json"), "w"), indent=1)
+    variants = []
+    for name, kind, args, over in VARIANTS:
+        n, e, w = make_instance(kind, args)
+        r = run_reference(binary, n, e, w, over=over)
+        r.update(name=name, kind=kind, args=list(args), n=n, edges=len(w), params=over)
+        variants.append(r)
+        print(name, "nodes", r["nodes"], "opt", r["opt"], "root %.9f" % r["bounds"][0], "evaluated", len(r["bounds"]))
+    json.dump({"generator": "tests/golden/make_golden.py", "reference_build": "oracle/ref/Makefile strict flavour",
+               "instances": variants}, open(os.path.join(HERE, "reference_bab_params.json"), "w"), indent=1)
 
 
 if __name__ == "__main__":

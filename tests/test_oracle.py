@@ -50,6 +50,25 @@ def test_oracle_reproduces_reference_branch_and_bound(orc, fx):
     assert max(abs(a - b) for a, b in zip(bounds, fx["bounds"])) <= 1e-9
 
 
+VARIANTS = json.load(open(os.path.join(HERE, "golden", "reference_bab_params.json")))["instances"]
+
+
+@pytest.mark.parametrize("fx", VARIANTS, ids=[f["name"] for f in VARIANTS])
+def test_oracle_reproduces_reference_trees_under_other_parameters(orc, fx):
+    """Reference trees under non-shipped settings (triangles only, no heptagons,
+    least-fractional branching, no diff give-up with sigma0 1.6, a fixed
+    triangle budget), node by node."""
+    n, e, w = _fixture_instance(fx)
+    SL = orc.build_L(n, (e, w))
+    c = orc.Ctx(orc.shipped_params(**fx["params"]), SL, n, rng=orc.RNG_GLIBC, topk=orc.TOPK_REFERENCE, canon_sign=0)
+    r = c.bab(max_nodes=2000)
+    bounds = [s.bound for s in r["log"]]
+    assert r["nodes"] == fx["nodes"] and r["opt"] == fx["opt"]
+    assert sorted(np.nonzero(r["sol"])[0].tolist()) == sorted(fx["sol"])
+    assert len(bounds) == len(fx["bounds"])
+    assert max(abs(a - b) for a, b in zip(bounds, fx["bounds"])) <= 1e-9
+
+
 def test_oracle_counter_mode_is_order_free(orc):
     """Counter streams: a node's bound does not depend on what was bounded before."""
     n, e, w = G.gnp(36, 0.5, "pm1", seed=21)
