@@ -65,9 +65,13 @@ def balance_plan(sizes):
     return plan
 
 
-def sharded_bab(ctx, new_node, dist=None, depth=2, max_nodes=100000, balance=True, info=None, batch=1):
+def sharded_bab(ctx, new_node, dist=None, depth=2, max_nodes=100000, balance=True, info=None, batch=1,
+                root_only=False, strategy=1):
     """Returns (optimum, solution vector, nodes evaluated on this rank, evaluated on all ranks).
-    info (a dict, optional) receives the number of rebalancing transfers and nodes moved."""
+    info (a dict, optional) receives the number of rebalancing transfers and nodes moved.
+    root_only: bound the root and stop (the reference's `root` parameter, main.c:106,195).
+    strategy: the reference's branchingStrategy (1 most fractional, 0 least fractional;
+    getBranchingVariable, bab_functions.c:389-423)."""
     rank = dist.get_rank() if dist else 0
     world = dist.get_world_size() if dist else 1
     pb = ctx.N - 1
@@ -92,7 +96,7 @@ def sharded_bab(ctx, new_node, dist=None, depth=2, max_nodes=100000, balance=Tru
     frontier = []  # unevaluated nodes: (parent bound, fixings)
 
     def children(b, fx, nd):
-        ic = _branch_var(nd, pb)
+        ic = _branch_var(nd, pb, strategy)
         out = []
         if ic >= 0 and ctx.lb()[0] + 1.0 < b:
             for v in (0, 1):
@@ -101,7 +105,7 @@ def sharded_bab(ctx, new_node, dist=None, depth=2, max_nodes=100000, balance=Tru
                 out.append((b, f2))
         return out
 
-    frontier = children(rb, {}, root)
+    frontier = [] if root_only else children(rb, {}, root)
     for _ in range(depth - 1):
         nxt = []
         for b, fx in frontier:
@@ -162,7 +166,7 @@ def sharded_bab(ctx, new_node, dist=None, depth=2, max_nodes=100000, balance=Tru
                 lb, sol = lb2, sol2
             for (fx, nd), b in zip(take, bounds):
                 if lb + 1.0 < b:
-                    ic = _branch_var(nd, pb)
+                    ic = _branch_var(nd, pb, strategy)
                     if ic < 0:  # every variable fixed: the node is a single cut, nothing to branch
                         continue
                     for v in (0, 1):

@@ -313,6 +313,32 @@ def test_sharded_branch_and_bound_on_gloo_ranks(orc, world, depth, batch):
         assert sizes and max(sizes) <= batch and max(sizes) > 1
 
 
+def test_sharded_root_only(orc):
+    """root_only bounds the root and stops, as the reference's `root` parameter."""
+    from madam_gb300.sharded import sharded_bab
+
+    n, e, w = G.gnp(40, 0.5, "pm1", seed=5)
+    c = orc.Ctx(orc.shipped_params(root=1), orc.build_L(n, (e, w)), n)
+    best, sol, mine, total = sharded_bab(c, lambda fx: orc.make_node(n - 1, fx), root_only=True)
+    ref = orc.Ctx(orc.shipped_params(root=1), orc.build_L(n, (e, w)), n).bab()
+    assert mine == total == 1 and best == ref["opt"] and ref["nodes"] == 1
+
+
+def test_sharded_least_fractional_branching(orc):
+    """branchingStrategy 0 through the sharded driver reaches the reference's
+    optimum on the least-fractional fixture tree."""
+    import json
+
+    from madam_gb300.sharded import sharded_bab
+
+    fx = [f for f in json.load(open(os.path.join(ROOT, "tests", "golden", "reference_bab_params.json")))["instances"]
+          if f["params"].get("branchingStrategy") == 0][0]
+    n, e, w = G.gnp(*fx["args"][:3], seed=fx["args"][3])
+    c = orc.Ctx(orc.shipped_params(**fx["params"]), orc.build_L(n, (e, w)), n)
+    best, sol, mine, total = sharded_bab(c, lambda f: orc.make_node(n - 1, f), strategy=0)
+    assert best == fx["opt"] and G.cut_value(n, e, w, sol) == fx["opt"]
+
+
 def test_balance_plan_properties():
     """On random queue sizes: receivers were empty, donors held nodes and keep at
     least one, nobody receives twice, nodes are conserved, and an empty rank is
