@@ -21,7 +21,9 @@ lb() -> (lb, sol) and an `N` attribute; `new_node(fixed)` builds a node with
 xfixed / sol / fracsol arrays (the BabNode layout).  With batch > 1 and a context
 that has bound_batch(nodes, rank) -> (bounds, stats) (the GPU library's), each rank
 pops up to `batch` open nodes per round and bounds them in one call, as the
-library's own driver does (pop-k / push-2k around mcb_bound_batch).
+library's own driver does (pop-k / push-2k around mcb_bound_batch).  The exchange
+runs on whatever process group `dist` holds: gloo with host tensors, or NCCL with
+tensors on the rank's current GPU (call torch.cuda.set_device first).
 """
 import heapq
 import itertools
@@ -76,12 +78,19 @@ def sharded_bab(ctx, new_node, dist=None, depth=2, max_nodes=100000, balance=Tru
     world = dist.get_world_size() if dist else 1
     pb = ctx.N - 1
 
+    # NCCL groups reduce device tensors (the rank's current GPU); gloo host tensors
+    dev = None
+    if dist and dist.get_backend() == "nccl":
+        import torch
+
+        dev = torch.device("cuda", torch.cuda.current_device())
+
     def allreduce(v, op):
         if not dist:
             return v
         import torch
 
-        t = torch.tensor([v], dtype=torch.float64)
+        t = torch.tensor([v], dtype=torch.float64, device=dev)
         dist.all_reduce(t, op=op)
         return float(t[0])
 
