@@ -42,10 +42,6 @@ def _branch_var(nd, pb, strategy=1):
     return ic
 
 
-def _fixed(nd, pb):
-    return {i: int(nd.sol[i]) for i in range(pb) if nd.xfixed[i]}
-
-
 def balance_plan(sizes):
     """Transfers [(donor, receiver, count)] that give every empty queue half of the
     currently largest non-empty one (donors are ranks that held nodes before the
