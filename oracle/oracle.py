@@ -5,7 +5,6 @@ Only the tests, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
 The product library never imports it.
 """
 import ctypes as C
-import os
 
 import numpy as np
 
