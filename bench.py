@@ -61,7 +61,8 @@ def _cpu_worker(args):
     prm = O.shipped_params(**wl["params"])
     out = []
     for i in idx_list:
-        oc = O.Ctx(prm, wl["SL"], wl["n"], rng=O.RNG_COUNTER, topk=O.TOPK_CANONICAL, canon_sign=1)
+        # the reference's own method: its rand() streams, top-K order and eigenvector signs
+        oc = O.Ctx(prm, wl["SL"], wl["n"], rng=O.RNG_GLIBC, topk=O.TOPK_REFERENCE, canon_sign=0)
         oc.set_lb(lb)
         nd = O.make_node(wl["n"] - 1, wl["fixings"][i])
         t0 = time.perf_counter()
@@ -332,7 +333,8 @@ def run_ours(a):
             c = json.loads(r.stdout.strip().splitlines()[-1])
             cpu = {"value": c["value"], "unit": UNIT, "cores": c["cores"], "kind": "port",
                    "sample": "%d of the workload's nodes, one per process, oracle (C restatement of the reference) "
-                             "with single-threaded OpenBLAS; %.1f s wall" % (c["nodes"], c["wall"])}
+                             "in the reference's mode (its rand() streams) with single-threaded OpenBLAS; %.1f s wall"
+                             % (c["nodes"], c["wall"])}
         except Exception:
             cpu = {"value": None, "unit": UNIT, "cores": None, "kind": "port", "sample": "failed: " + r.stderr[-300:]}
     admm = sum(s.admm_iters for st in stats for s in st)
@@ -386,7 +388,8 @@ def _tto_worker(rank, world, port, q):
     from oracle import oracle as O
 
     n, e, w = G.gnp(TTO["n"], TTO["p"], TTO["weights"], seed=TTO["seed"])
-    ctx = O.Ctx(O.shipped_params(**TTO["params"]), O.build_L(n, (e, w)), n)
+    ctx = O.Ctx(O.shipped_params(**TTO["params"]), O.build_L(n, (e, w)), n, rng=O.RNG_GLIBC,
+                topk=O.TOPK_REFERENCE, canon_sign=0)
     t0 = time.perf_counter()
     best, _, mine, total = sharded_bab(ctx, lambda fx: O.make_node(n - 1, fx), dist=dist, depth=3)
     q.put((rank, best, mine, total, time.perf_counter() - t0))
@@ -417,8 +420,8 @@ def cpu_time_to_optimum(cores):
                                                                         TTO["seed"]),
             "seconds": max(r[4] for r in res), "wall_with_process_start": wall, "optimum": best,
             "nodes": int(res[0][3]), "cores": cores,
-            "method": "oracle port of the reference on one process per core (gloo), best-first per rank, "
-                      "shared incumbent, queue rebalancing"}
+            "method": "oracle port of the reference in its reference mode on one process per core (gloo), "
+                      "best-first per rank, shared incumbent, queue rebalancing"}
 
 
 def run_reference(a):
@@ -442,7 +445,8 @@ def run_reference(a):
         "config": {"workload": a.workload, "nodes_per_step": ns},
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": "%d nodes per step, one process per core, oracle (C restatement of the "
-                                   "reference, checked bit-for-bit against it) with single-threaded OpenBLAS" % ns},
+                                   "reference, checked bit-for-bit against it) in the reference's mode (its rand() "
+                                   "streams) with single-threaded OpenBLAS" % ns},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     if not a.no_compare:
