@@ -94,6 +94,39 @@ def test_rudy_files_read_like_the_reference(tmp_path):
     libc.fflush(None)  # readData's printf output, inside the test's capture
 
 
+@pytest.mark.skipif(not (os.path.isdir(os.path.join(REF, "Instances")) and
+                         os.path.exists(os.path.join(ROOT, "oracle", "_ref", "libmadam_ref_strict.so"))),
+                    reason="reference instances or build not present")
+def test_published_instances_read_like_the_reference():
+    """All 220 instance files shipped with the reference (130 rudy graphs of 100
+    vertices and the 90 of the rudy_150 families) give the same SP->L through
+    read_rudy + extended_laplacian as through readData, bit for bit."""
+    import ctypes as C
+    import glob
+
+    R = C.CDLL(os.path.join(ROOT, "oracle", "_ref", "libmadam_ref_strict.so"))
+    libc = C.CDLL(None)
+    libc.fopen.restype = C.c_void_p
+    libc.fopen.argtypes = [C.c_char_p, C.c_char_p]
+    C.c_void_p.in_dll(R, "output").value = libc.fopen(os.devnull.encode(), b"w")
+
+    class Problem(C.Structure):  # admm.h:121-127
+        _fields_ = [("L", C.POINTER(C.c_double)), ("n", C.c_int), ("NIneq", C.c_int), ("NPentIneq", C.c_int),
+                    ("NHeptaIneq", C.c_int)]
+
+    SP = C.POINTER(Problem).in_dll(R, "SP")
+    files = sorted(f for f in glob.glob(os.path.join(REF, "Instances", "**", "*"), recursive=True)
+                   if os.path.isfile(f) and ".output" not in f and not f.endswith((".md", ".txt", ".py")))
+    assert len(files) >= 220
+    for f in files:
+        assert R.readData(f.encode()) == 0, f
+        k = SP.contents.n
+        ref = np.ctypeslib.as_array(SP.contents.L, shape=(k * k,)).copy()
+        n, e, w = G.read_rudy(f)
+        assert np.array_equal(G.extended_laplacian(n, e, w).ravel(order="F"), ref), f
+    libc.fflush(None)
+
+
 def test_rudy_roundtrip(tmp_path):
     n, e, w = G.gnp(20, 0.5, "int10", seed=4)
     f = tmp_path / "g.rudy"
