@@ -98,9 +98,9 @@ def test_rudy_files_read_like_the_reference(tmp_path):
                          os.path.exists(os.path.join(ROOT, "oracle", "_ref", "libmadam_ref_strict.so"))),
                     reason="reference instances or build not present")
 def test_published_instances_read_like_the_reference():
-    """All 220 instance files shipped with the reference (130 rudy graphs of 100
-    vertices and the 90 of the rudy_150 families) give the same SP->L through
-    read_rudy + extended_laplacian as through readData, bit for bit."""
+    """All 220 instance files shipped with the reference (130 rudy graphs of 60, 80
+    and 100 vertices and the 90 of the rudy_150 families) give the same SP->L
+    through read_rudy + extended_laplacian as through readData, bit for bit."""
     import ctypes as C
     import glob
 
