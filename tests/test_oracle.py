@@ -127,6 +127,39 @@ def test_oracle_root_bounds_near_published(orc):
         assert abs(b - root) <= 1e-3 * root
 
 
+REF_BIN = os.path.join(os.path.dirname(HERE), "oracle", "_ref", "madam_ref_strict")
+
+
+@pytest.mark.skipif(not (os.path.isdir(os.path.join(REF, "Instances")) and os.path.exists(REF_BIN)),
+                    reason="reference instances or build not present")
+def test_oracle_root_bounds_match_the_reference_on_shipped_instances(orc, tmp_path):
+    """One shipped instance of each family (g05, pm1d, pm1s, pw01, pw05, pw09, w01,
+    w05, w09 at n = 60..100): the root bound of the reference's strict build and of
+    the oracle in reference mode agree to 1e-12 relative.  The instance is copied
+    first, since the reference writes its .output report beside its input."""
+    import shutil
+    import subprocess
+
+    from madam_gb300 import lib as M
+
+    prm = tmp_path / "params"
+    prm.write_text("".join("%s = %s\n" % kv for kv in M.SHIPPED.items()))
+    picks = ["g05_60.3", "pm1d_100.9", "pm1s_80.5", "pw01_100.8", "pw05_100.2", "pw09_100.1", "w01_100.4",
+             "w05_100.7", "w09_100.0"]
+    for name in picks:
+        src = os.path.join(REF, "Instances", "rudy", name)
+        inst = str(tmp_path / name)
+        shutil.copyfile(src, inst)
+        out = subprocess.run([REF_BIN, inst, str(prm), "1"], capture_output=True, text=True, cwd=str(tmp_path),
+                             timeout=600).stdout
+        ref = float(re.search(r"^node 1 level 0 n \d+ bound (\S+)", out, re.M).group(1))
+        n, e, w = G.read_rudy(inst)
+        c = orc.Ctx(orc.shipped_params(), orc.build_L(n, (e, w)), n, rng=orc.RNG_GLIBC, topk=orc.TOPK_REFERENCE,
+                    canon_sign=0)
+        got = c.bab(max_nodes=1)["log"][0].bound
+        assert abs(got - ref) <= 1e-12 * abs(ref), (name, got, ref)
+
+
 # ---- numpy restatements of the operators ------------------------------------
 def _np_op_B(X, tri, pent, hept):
     y = []
