@@ -26,9 +26,10 @@
 // the accumulators (32 lanes each) with tcgen05.ld, through shared-memory tiles
 // (row-major for the direct half, column-major for the mirror) so that every
 // global store is coalesced and 64 or 128 bits wide.  Every wait on an
-// mbarrier is bounded: on expiry the CTA records an error code and skips the
-// rest.  Compiled with MCB_TC_TRACE, CTA (0, 0) records globaltimer stamps of
-// its phases (read by mcb_tc_trace) for latency studies.
+// mbarrier is bounded: on expiry the CTA records an error code, gives the TMA
+// loads it still has in flight their own bounded wait, skips the rest and
+// releases its tensor memory.  Compiled with MCB_TC_TRACE, CTA (0, 0) records
+// globaltimer stamps of its phases (read by mcb_tc_trace) for latency studies.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -217,6 +218,7 @@ __global__ void __launch_bounds__(128, 3 - kStages) k_tc_gemm(const __grid_const
 
     if (tid == 0) {
         const uint32_t idesc = instr_desc(BM, BN);
+        int issued = 0, landed = 0;  // chunks whose loads were issued / have been waited for
         auto load = [&](int kc) {
             const int s = kc % kStages;
             unsigned char *st = smem + s * kStageBytes;
@@ -225,6 +227,7 @@ __global__ void __launch_bounds__(128, 3 - kStages) k_tc_gemm(const __grid_const
                 tma_load_3d(st + p * kTileBytes, &maps.a[p], kc * BK, m0, slot, &full[s]);
                 tma_load_3d(st + (kPieces + p) * kTileBytes, &maps.b[p], kc * BK, n0, slot, &full[s]);
             }
+            ++issued;
         };
         bool ok = true;
         for (int kc = 0; kc < kStages && kc < nk; ++kc) load(kc);
@@ -233,6 +236,7 @@ __global__ void __launch_bounds__(128, 3 - kStages) k_tc_gemm(const __grid_const
             const uint32_t use = (uint32_t)(kc / kStages) & 1u;
             ok = mbar_wait(&full[s], use);
             if (!ok) break;
+            ++landed;
             trace(2 + 2 * kc);
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             const uint32_t base = smem_u32(smem + s * kStageBytes);
@@ -257,7 +261,12 @@ __global__ void __launch_bounds__(128, 3 - kStages) k_tc_gemm(const __grid_const
                 load(kc + kStages);
             }
         }
-        if (!ok) s_fail = 1;
+        if (!ok) {
+            s_fail = 1;
+            // loads still in flight write this CTA's shared memory: give them their
+            // own bounded wait before the block can exit and the memory is reused
+            for (int j = landed; j < issued; ++j) mbar_wait(&full[j % kStages], (uint32_t)(j / kStages) & 1u);
+        }
         mma_commit(done);
     }
     __syncwarp();
