@@ -10,12 +10,30 @@
  * mcb_params and mcb_bab_node have the layouts of Parameters and BabNode, so
  * the reference's objects are passed as they are.  The context is created on
  * the first call from SP (the reference keeps one problem per process). */
+#include <stddef.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 
 #include "admm.h"
 #include "mcbound.h"
+
+/* The casts below are valid only while the layouts agree: checked field by field
+ * at compile time, for Parameters through the reference's own field list
+ * (PARAM_FIELDS, admm.h:58-81) and for BabNode (admm.h:147-155). */
+_Static_assert(sizeof(mcb_params) == sizeof(Parameters), "mcb_params differs from Parameters");
+#define P(type, name, format, def_value)                                                       \
+    _Static_assert(offsetof(mcb_params, name) == offsetof(Parameters, name), "Parameters." #name); \
+    _Static_assert(sizeof(((mcb_params *)0)->name) == sizeof(type), "Parameters." #name " type");
+PARAM_FIELDS
+#undef P
+_Static_assert(sizeof(mcb_bab_node) == sizeof(BabNode), "mcb_bab_node differs from BabNode");
+_Static_assert(offsetof(mcb_bab_node, xfixed) == offsetof(BabNode, xfixed), "BabNode.xfixed");
+_Static_assert(offsetof(mcb_bab_node, sol) == offsetof(BabNode, sol.X), "BabNode.sol");
+_Static_assert(offsetof(mcb_bab_node, fracsol) == offsetof(BabNode, fracsol), "BabNode.fracsol");
+_Static_assert(offsetof(mcb_bab_node, level) == offsetof(BabNode, level), "BabNode.level");
+_Static_assert(offsetof(mcb_bab_node, upper_bound) == offsetof(BabNode, upper_bound), "BabNode.upper_bound");
+_Static_assert(MCB_NMAX == NMAX, "NMAX");
 
 /* The one routine of operators.c that the kept files call: readData builds the
  * Laplacian with it (process_input.c:265-268).  X = diagonal matrix of y, n x n,
