@@ -159,8 +159,8 @@ struct mcb_ctx {
     // host-side wall time per phase of bound_batch (seconds)
     double host_s[8] = {};
     // instrumentation
-    long long h2d = 0, d2h = 0;
-    long long lib_launches = 0;        // cuBLAS launches (not counted as own kernels)        // host<->device bytes moved by the bound calls
+    long long h2d = 0, d2h = 0;        // host<->device bytes moved by the bound calls
+    long long lib_launches = 0;        // cuBLAS launches (not counted as own kernels)
     double work[K_NCLASS] = {};        // algorithmic work per class (flops or bytes, see kWorkUnit)
     long long launches[K_NCLASS] = {};
     double ms[K_NCLASS] = {};
