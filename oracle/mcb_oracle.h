@@ -129,6 +129,11 @@ void orc_op_Bt(int n, double *X, int ntri, const int *tri, int npent, const int 
 int orc_project(int n, const double *W, double *Xp, double *Q, double *Z, double *evals, int canon_sign);
 /* dsyevr ABSTOL used by orc_project / orc_lambda_max (default 1e-8 as the reference) */
 void orc_set_abstol(double abstol);
+/* Newton-Schulz projection model: with k > 0 steps (p_i(x) = a_i x + b_i x^3), orc_project
+ * returns the sign-iteration projection in exact arithmetic instead of the reference's:
+ * X_+ = sum_j lambda_j (1 + p_k(...p_1(lambda_j / ||W||_F))) / 2 v_j v_j^T over all eigenpairs
+ * (Z and M stay the reference's).  k = 0 restores the reference projection. */
+void orc_set_ns_schedule(int k, const double *a, const double *b);
 /* largest eigenvalue as admm.c:731-752 computes it */
 double orc_lambda_max(int n, const double *A);
 /* basic SDP bound by the predictor-corrector IPM (ipm_mc_pk.c); returns iterations or -1 */

@@ -80,6 +80,7 @@ def lib():
     L.orc_op_Bt.argtypes = [C.c_int, _dp, C.c_int, _ip, C.c_int, _ip, C.c_int, _ip, _dp]
     L.orc_project.argtypes = [C.c_int, _dp, _dp, _dp, _dp, _dp, C.c_int]
     L.orc_set_abstol.argtypes = [C.c_double]
+    L.orc_set_ns_schedule.argtypes = [C.c_int, C.c_void_p, C.c_void_p]
     L.orc_lambda_max.restype = C.c_double
     L.orc_lambda_max.argtypes = [C.c_int, _dp]
     L.orc_ipm.argtypes = [_dp, C.c_int, _dp, _dp, _dp, C.POINTER(C.c_double)]
@@ -274,6 +275,17 @@ def project(W, canon_sign=1, abstol=1e-8):
         raise RuntimeError("dsyevr failed")
     return (Xp.reshape(n, n, order="F"), Q.reshape(n, n, order="F"),
             Z[: n * M].reshape(n, M, order="F"), ev[:M].copy())
+
+
+def set_ns_schedule(steps=None):
+    """Model the Newton-Schulz projection in exact arithmetic: steps = [(a, b), ...] of
+    p(x) = a x + b x^3; None restores the reference projection (see orc_set_ns_schedule)."""
+    if not steps:
+        lib().orc_set_ns_schedule(0, None, None)
+        return
+    a = np.ascontiguousarray([s[0] for s in steps], dtype=np.float64)
+    b = np.ascontiguousarray([s[1] for s in steps], dtype=np.float64)
+    lib().orc_set_ns_schedule(len(steps), a.ctypes.data, b.ctypes.data)
 
 
 def lambda_max(A, abstol=1e-8):

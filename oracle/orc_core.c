@@ -339,6 +339,13 @@ void orc_set_work_n(int N) { orc_work_n = N; }
  * counter (GPU-matching) form asks for full precision (0). */
 static double orc_abstol = 1e-8;
 void orc_set_abstol(double a) { orc_abstol = a; }
+/* Newton-Schulz projection model (mcb_oracle.h); off while ns_k == 0 */
+static int ns_k = 0;
+static double ns_a[64], ns_b[64];
+void orc_set_ns_schedule(int k, const double *a, const double *b) {
+    ns_k = k < 0 ? 0 : (k > 64 ? 64 : k);
+    for (int i = 0; i < ns_k; ++i) { ns_a[i] = a[i]; ns_b[i] = b[i]; }
+}
 
 int orc_project(int n, const double *W, double *Xp, double *Q, double *Z, double *evals,
                 int canon_sign) {
@@ -386,8 +393,34 @@ int orc_project(int n, const double *W, double *Xp, double *Q, double *Z, double
     }
     /* X_+ = Z Z^T on the lower triangle; the upper triangle keeps W's values */
     memcpy(Xp, W, nn * sizeof(double));
-    double one = 1.0, zero = 0.0;
-    if (M > 0) {
+    double one = 1.0, zero = 0.0, mone = -1.0;
+    if (ns_k > 0) {
+        /* the sign iteration in exact arithmetic: every eigenvalue's step function becomes the
+         * composed step polynomials at lambda / ||W||_F; positive and negative weights in two SYRKs */
+        double *B = malloc(nn * sizeof(double)), *V = malloc(nn * sizeof(double));
+        double *ev = malloc((size_t)n * sizeof(double));
+        double *Vp = malloc(nn * sizeof(double)), *Vn = malloc(nn * sizeof(double));
+        memcpy(B, W, nn * sizeof(double));
+        int Ma = 0, info2 = 0, np_ = 0, nm_ = 0;
+        double za = 0.0;
+        orc_la.dsyevr("V", "A", "L", &n, B, &n, &VL, &VU, &IL, &IU, &za, &Ma, ev, V, &n, isuppz,
+                      work, &lwork, iwork, &liwork, &info2, 1, 1, 1);
+        for (int j = 0; j < Ma && info2 == 0; ++j) {
+            double x = nfro > 0 ? ev[j] / nfro : 0.0;
+            for (int k = 0; k < ns_k; ++k) x = ns_a[k] * x + ns_b[k] * x * x * x;
+            double wgt = ev[j] * (1.0 + x) / 2.0;
+            double *dst = wgt > 0 ? Vp + (size_t)np_++ * n : (wgt < 0 ? Vn + (size_t)nm_++ * n : NULL);
+            if (!dst) continue;
+            double sc = sqrt(fabs(wgt));
+            for (int i = 0; i < n; ++i) dst[i] = V[i + (size_t)j * n] * sc;
+        }
+        for (int j = 0; j < n; ++j)
+            for (int i = j; i < n; ++i) Xp[i + (size_t)j * n] = 0.0;
+        if (np_) orc_la.dsyrk("L", "N", &n, &np_, &one, Vp, &n, &one, Xp, &n, 1, 1);
+        if (nm_) orc_la.dsyrk("L", "N", &n, &nm_, &mone, Vn, &n, &one, Xp, &n, 1, 1);
+        free(B); free(V); free(ev); free(Vp); free(Vn);
+        if (info2 != 0) { free(A); free(work); free(iwork); free(isuppz); return -1; }
+    } else if (M > 0) {
         orc_la.dsyrk("L", "N", &n, &M, &one, Z, &n, &zero, Xp, &n, 1, 1);
     } else {
         for (int j = 0; j < n; ++j)

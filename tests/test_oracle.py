@@ -160,6 +160,30 @@ def test_oracle_root_bounds_match_the_reference_on_shipped_instances(orc, tmp_pa
         assert abs(got - ref) <= 1e-12 * abs(ref), (name, got, ref)
 
 
+def test_newton_schulz_model_l0_truncation(orc, gpu_lib):
+    """The chosen form's sign iteration in exact arithmetic (the oracle's projection
+    model; the schedule is the library's, host arithmetic only): with l0 = 1e-6 and
+    1e-5 the ADMM runs the same iterations as with the exact projection and the
+    bound moves by less than 1e-8 -- the truncation costs nothing at either l0."""
+    n, e, w = G.gnp(64, 0.5, "pm1", seed=4)
+    SL = orc.build_L(n, (e, w))
+    prm = orc.shipped_params(include_Hepta=0, use_diff=0)
+    out = {}
+    try:
+        for l0 in (None, 1e-6, 1e-5):
+            orc.set_ns_schedule(None if l0 is None else [(a, b) for a, b, _ in gpu_lib.ns_schedule_for(l0)])
+            c = orc.Ctx(prm, SL, n)
+            b, st = c.evaluate(orc.make_node(n - 1), rank=1)
+            out[l0] = (b, st.admm_iters)
+    finally:
+        orc.set_ns_schedule(None)
+    b0, it0 = out[None]
+    assert it0 > 0
+    for l0 in (1e-6, 1e-5):
+        assert out[l0][1] == it0, out
+        assert abs(out[l0][0] - b0) <= 1e-8 * abs(b0), out
+
+
 # ---- numpy restatements of the operators ------------------------------------
 def _np_op_B(X, tri, pent, hept):
     y = []
