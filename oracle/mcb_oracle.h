@@ -134,6 +134,8 @@ void orc_set_abstol(double abstol);
  * X_+ = sum_j lambda_j (1 + p_k(...p_1(lambda_j / ||W||_F))) / 2 v_j v_j^T over all eigenpairs
  * (Z and M stay the reference's).  k = 0 restores the reference projection. */
 void orc_set_ns_schedule(int k, const double *a, const double *b);
+/* relative residual at which the ADMM's linear solve stops (default 1e-15; <= 0 restores it) */
+void orc_set_cg_tol(double tol);
 /* largest eigenvalue as admm.c:731-752 computes it */
 double orc_lambda_max(int n, const double *A);
 /* basic SDP bound by the predictor-corrector IPM (ipm_mc_pk.c); returns iterations or -1 */

@@ -81,6 +81,7 @@ def lib():
     L.orc_project.argtypes = [C.c_int, _dp, _dp, _dp, _dp, _dp, C.c_int]
     L.orc_set_abstol.argtypes = [C.c_double]
     L.orc_set_ns_schedule.argtypes = [C.c_int, C.c_void_p, C.c_void_p]
+    L.orc_set_cg_tol.argtypes = [C.c_double]
     L.orc_lambda_max.restype = C.c_double
     L.orc_lambda_max.argtypes = [C.c_int, _dp]
     L.orc_ipm.argtypes = [_dp, C.c_int, _dp, _dp, _dp, C.POINTER(C.c_double)]
@@ -286,6 +287,11 @@ def set_ns_schedule(steps=None):
     a = np.ascontiguousarray([s[0] for s in steps], dtype=np.float64)
     b = np.ascontiguousarray([s[1] for s in steps], dtype=np.float64)
     lib().orc_set_ns_schedule(len(steps), a.ctypes.data, b.ctypes.data)
+
+
+def set_cg_tol(tol=None):
+    """Relative residual of the ADMM's linear solve (None: the default 1e-15)."""
+    lib().orc_set_cg_tol(tol if tol else 0.0)
 
 
 def lambda_max(A, abstol=1e-8):

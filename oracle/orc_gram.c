@@ -64,6 +64,10 @@ void orc_gram_free(orc_gram *G) {
     G->rp = NULL; G->ci = NULL; G->v = NULL;
 }
 
+/* squared relative residual at which the solve stops (1e-15 by default) */
+static double gram_tol2 = 1e-30;
+void orc_set_cg_tol(double tol) { gram_tol2 = tol > 0 ? tol * tol : 1e-30; }
+
 void orc_gram_solve(const orc_gram *G, const double *b, double *x) {
     int m = G->m;
     double *r = malloc(((size_t)m + 1) * sizeof(double)), *p = malloc(((size_t)m + 1) * sizeof(double));
@@ -71,7 +75,7 @@ void orc_gram_solve(const orc_gram *G, const double *b, double *x) {
     double bb = 0.0;
     for (int i = 0; i < m; ++i) { x[i] = 0.0; r[i] = b[i]; p[i] = b[i]; bb += b[i] * b[i]; }
     double rr = bb;
-    for (int it = 0; it < 10000 && bb > 0.0 && rr > 1e-30 * bb; ++it) {
+    for (int it = 0; it < 10000 && bb > 0.0 && rr > gram_tol2 * bb; ++it) {
         double pq = 0.0;
         for (int i = 0; i < m; ++i) {
             double acc = 0.0;

@@ -184,6 +184,27 @@ def test_newton_schulz_model_l0_truncation(orc, gpu_lib):
         assert abs(out[l0][0] - b0) <= 1e-8 * abs(b0), out
 
 
+def test_linear_solve_tolerance_slack(orc, gpu_lib):
+    """Under the chosen form's projection model (l0 = 1e-6), solving (B B^T + I) t = r
+    to 1e-8 instead of the chosen form's 1e-10 leaves the ADMM's iterations unchanged
+    and the bound within 1e-8."""
+    n, e, w = G.gnp(64, 0.5, "pm1", seed=4)
+    SL = orc.build_L(n, (e, w))
+    prm = orc.shipped_params(include_Hepta=0, use_diff=0)
+    out = {}
+    try:
+        orc.set_ns_schedule([(a, b) for a, b, _ in gpu_lib.ns_schedule_for(1e-6)])
+        for tol in (1e-10, 1e-8):
+            orc.set_cg_tol(tol)
+            b, st = orc.Ctx(prm, SL, n).evaluate(orc.make_node(n - 1), rank=1)
+            out[tol] = (b, st.admm_iters)
+    finally:
+        orc.set_ns_schedule(None)
+        orc.set_cg_tol(None)
+    assert out[1e-8][1] == out[1e-10][1] > 0, out
+    assert abs(out[1e-8][0] - out[1e-10][0]) <= 1e-8 * abs(out[1e-10][0]), out
+
+
 # ---- numpy restatements of the operators ------------------------------------
 def _np_op_B(X, tri, pent, hept):
     y = []
