@@ -51,44 +51,71 @@ def _args():
 
 
 # ---------------------------------------------------------------------------
-# CPU side: the oracle (the reference's method restated in C) on host cores
-def _cpu_worker(args):
-    wl_name, idx_list, lb = args
+# CPU side: the oracle (the reference's method restated in C) on host cores.
+# A pool of spawned processes, one per core, is created once: every worker
+# imports the oracle and builds the workload in its initializer, so process
+# start-up stays outside every timed region.  Each task bounds one node of the
+# workload's node list with a fresh oracle context in the reference's own mode
+# (its rand() streams, top-K order and eigenvector signs) and single-threaded
+# BLAS, as the reference runs one node per MPI process (setupenv.sh:6-8).
+_POOL_STATE = {}
+
+
+def _pool_init(wl_name):
+    for v in ("OPENBLAS_NUM_THREADS", "GOTO_NUM_THREADS", "OMP_NUM_THREADS"):
+        os.environ[v] = "1"
     from madam_gb300 import workload as W
     from oracle import oracle as O
 
     wl = W.make(wl_name)
-    prm = O.shipped_params(**wl["params"])
-    out = []
-    for i in idx_list:
-        # the reference's own method: its rand() streams, top-K order and eigenvector signs
-        oc = O.Ctx(prm, wl["SL"], wl["n"], rng=O.RNG_GLIBC, topk=O.TOPK_REFERENCE, canon_sign=0)
-        oc.set_lb(lb)
-        nd = O.make_node(wl["n"] - 1, wl["fixings"][i])
+    _POOL_STATE.update(wl=wl, O=O, prm=O.shipped_params(**wl["params"]))
+    O.lib()
+
+
+def _pool_bound(i):
+    wl, O = _POOL_STATE["wl"], _POOL_STATE["O"]
+    oc = O.Ctx(_POOL_STATE["prm"], wl["SL"], wl["n"], rng=O.RNG_GLIBC, topk=O.TOPK_REFERENCE, canon_sign=0)
+    oc.set_lb(wl["lb"], wl["lb_sol"])
+    nd = O.make_node(wl["n"] - 1, wl["fixings"][i])
+    t0 = time.perf_counter()
+    b, _ = oc.evaluate(nd, rank=1)
+    dt = time.perf_counter() - t0
+    oc.close()
+    return i, b, dt
+
+
+class CpuPool:
+    """One oracle process per host core, started once, bounding nodes of one workload."""
+
+    def __init__(self, wl_name, cores):
+        self.cores = cores
+        self.pool = mp.get_context("spawn").Pool(cores, initializer=_pool_init, initargs=(wl_name,))
+
+    def run(self, idx):
         t0 = time.perf_counter()
-        b, st = oc.evaluate(nd, rank=1)
-        out.append((i, b, time.perf_counter() - t0))
-        oc.close()
-    return out
+        res = self.pool.map(_pool_bound, list(idx), chunksize=1)
+        wall = time.perf_counter() - t0
+        return dict(nodes=len(res), wall=wall, node_seconds=[r[2] for r in res], bounds=[r[1] for r in res])
+
+    def close(self):
+        self.pool.close()
+        self.pool.join()
 
 
 def cpu_sample(wl_name, nodes, cores):
-    # single-threaded BLAS per process, as the reference runs it (setupenv.sh:6-8)
-    for v in ("OPENBLAS_NUM_THREADS", "GOTO_NUM_THREADS", "OMP_NUM_THREADS"):
-        os.environ[v] = "1"
+    """A bounded sample on all host cores: `nodes` nodes of the workload (after one
+    untimed round of one node per core that starts the workers)."""
     from madam_gb300 import workload as W
 
-    wl = W.make(wl_name)
-    nodes = min(nodes, len(wl["fixings"]))
-    chunks = [[i] for i in range(nodes)]
-    ctx = mp.get_context("spawn")
-    t0 = time.perf_counter()
-    with ctx.Pool(cores) as pool:
-        res = pool.map(_cpu_worker, [(wl_name, c, wl["lb"]) for c in chunks])
-    wall = time.perf_counter() - t0
-    per = [r for rr in res for r in rr]
-    return dict(nodes=nodes, wall=wall, cores=cores, value=nodes / wall,
-                node_seconds=statistics.mean(p[2] for p in per))
+    nodes = min(nodes, W.WORKLOADS[wl_name]["nodes"])
+    pool = CpuPool(wl_name, cores)
+    try:
+        pool.run(range(min(cores, nodes)))
+        r = pool.run(range(nodes))
+    finally:
+        pool.close()
+    return dict(nodes=r["nodes"], wall=r["wall"], cores=cores, value=r["nodes"] / r["wall"],
+                node_seconds=statistics.mean(r["node_seconds"]))
 
 
 def host_cores():
@@ -162,6 +189,63 @@ FORMS = {"learned": "Newton-Schulz projection (BF16 split operands, FP64 product
 TTO = dict(n=100, p=0.5, weights="one", seed=1101, params=dict(include_Pent=0, include_Hepta=0))
 
 
+DTYPES = {"learned": "bf16 split (FP32-accurate) + f64", "mixed": "bf16 split (FP32-accurate) + f64", "fp64": "f64"}
+N512 = "gnp512_int10"
+
+
+def n512_block(torch, M, stream, form, nodes=16, cap_s=60.0):
+    """The n = 512 configuration (G(512, 0.1), integer weights in [-10, 10], all
+    three cut families): node throughput of the chosen form and of the plain FP64
+    form on the same nodes, the largest relative difference between their bounds,
+    and a time-capped branch-and-bound of the whole graph in both forms.  The tree
+    does not close within minutes (the root bound lies ~20% above the best cut), so
+    a capped run reports the gap it closed: (root bound - largest open bound) /
+    (root bound - incumbent)."""
+    from madam_gb300 import workload as W
+
+    wl = W.make(N512)
+    prm = M.params(**wl["params"])
+    base_trials = (prm.Pent_Trials, prm.Hepta_Trials)
+    fixes = wl["fixings"][:nodes]
+    out = {"workload": N512, "n": wl["n"], "nodes_per_step": len(fixes)}
+    bounds = {}
+    for f in (form, "fp64"):
+        ctx = _context(M, prm, wl["SL"], wl["n"], len(fixes), f, stream.cuda_stream, profile=False)
+
+        def step(ctx=ctx):
+            ctx.set_trials(*base_trials)
+            ctx.set_lb(wl["lb"], wl["lb_sol"])
+            b, st = ctx.bound_batch([M.node(x) for x in fixes], rank=1)
+            bounds[f] = b
+            return st
+        warm = 1 if f != "fp64" else 0
+        d, w, st, _ = _time_steps(torch, ctx, step, stream, 1, warm)
+        ctx.close()
+        out[f] = {"value": len(fixes) / d, "unit": UNIT, "steps": 1, "warmup": warm,
+                  "admm_iters": sum(s.admm_iters for s in st[0])}
+    rel = [abs(x - y) / abs(y) for x, y in zip(bounds[form], bounds["fp64"])]
+    out["speedup_vs_plain_fp64"] = out[form]["value"] / out["fp64"]["value"]
+    out["bound_rel_diff_vs_fp64"] = {"max": max(rel), "mean": statistics.mean(rel)}
+    tto = {"cap_seconds": cap_s, "batch": 64}
+    for f in (form, "fp64"):
+        tc = _context(M, prm, wl["SL"], wl["n"], 64, f, profile=False)
+        tc.set_time_limit(cap_s)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = tc.bab(batch=64, max_nodes=0)
+        sec = time.perf_counter() - t0
+        tc.close()
+        rec = {"seconds": sec, "nodes": r["nodes"], "incumbent": r["opt"], "root_bound": r["root_bound"],
+               "closed": not r["stopped"]}
+        if r["stopped"]:
+            ob = r["open_bound"] if r["open_bound"] is not None else r["opt"]
+            rec.update(time_to_optimum="> %.0f s" % cap_s, open_bound=ob, open_nodes=r["open_nodes"],
+                       gap_closed=(r["root_bound"] - ob) / max(1e-9, r["root_bound"] - r["opt"]))
+        tto[f] = rec
+    out["time_capped_bab"] = tto
+    return out
+
+
 def _context(M, prm, SL, n, batch, form, stream=None, profile=True):
     flags = M.PROJ_FP64 if form == "fp64" else M.PROJ_NS_BF16
     if form == "learned":
@@ -202,10 +286,18 @@ def _time_steps(torch, ctx, step, stream, steps, warmup, dist=None, clocks=None)
     return ev0.elapsed_time(ev1) / 1e3, wall, stats, clk
 
 
-# DRAM bytes (read + write) per launch of a kernel class, from one ncu capture of that
-# workload (summarised under profiles/); other workloads report null
-TRAFFIC = {("gnp256_pm1_batch64", "ns_gemm"): (25.24e6 + 0.036e6, "profiles/k_tc_gemm_gnp256_pm1_batch64.md, "
-                                               "warm launch, 64 nodes")}
+def traffic_from_profiles(workload, cls):
+    """DRAM bytes (read + write) per launch of a kernel class on a workload, from the
+    ncu summaries under profiles/ (a line `roofline-traffic: class=C workload=W
+    bytes=B` beside the capture it was read from); (bytes, file) or None."""
+    import glob
+    import re
+
+    for f in sorted(glob.glob(os.path.join(HERE, "profiles", "*.md"))):
+        for m in re.finditer(r"^roofline-traffic: class=(\S+) workload=(\S+) bytes=(\S+)", open(f).read(), re.M):
+            if m.group(1) == cls and m.group(2) == workload:
+                return float(m.group(3)), os.path.relpath(f, HERE)
+    return None
 
 
 def _roofline(M, ks, kw, workload=None):
@@ -216,9 +308,10 @@ def _roofline(M, ks, kw, workload=None):
         return None
     name, (nl, ms) = max(counted.items(), key=lambda kv: kv[1][1])
     work, unit = kw[name]
-    tr = TRAFFIC.get((workload, name))
+    tr = traffic_from_profiles(workload, name)
     base = {"kernel": name, "launches": nl, "ms_total": ms, "traffic": tr[0] if tr else None,
-            "traffic_unit": "bytes per launch" if tr else None, "traffic_source": tr[1] if tr else None}
+            "traffic_unit": "bytes per launch" if tr else None,
+            "traffic_source": ("ncu capture summarised in " + tr[1]) if tr else None}
     if unit == 1:
         peak = M.fp64_peak_gflops() / 1e3
         ach = work / (ms / 1e3) / 1e12
@@ -300,10 +393,10 @@ def run_ours(a):
     roof = _roofline(M, ks, kw, a.workload)
     tot_ms = sum(x[1] for x in ks.values())
     share = {k: round(v[1] / max(1e-9, tot_ms), 4) for k, v in ks.items() if v[1] > 0}
-    plain = tto = None
+    plain = tto = n512 = None
     if not a.no_compare and a.form != "fp64":
         # the plain FP64 form on the same workload (one warm-up, one timed step)
-        pc = _context(M, prm, wl["SL"], wl["n"], batch, "fp64", stream.cuda_stream)
+        pc = _context(M, prm, wl["SL"], wl["n"], batch, "fp64", stream.cuda_stream, profile=False)
         pd, pw, pst, _ = _time_steps(torch, pc, make_step(pc), stream, 1, 1)
         pc.close()
         plain = {"value": batch / pd, "unit": UNIT, "ms_per_step": pd * 1e3, "steps": 1, "warmup": 1,
@@ -323,32 +416,25 @@ def run_ours(a):
             tc.close()
         tto["speedup"] = tto["fp64"]["seconds"] / tto[a.form]["seconds"]
         tto["same_optimum"] = tto["fp64"]["optimum"] == tto[a.form]["optimum"]
+        if a.workload != N512:
+            n512 = n512_block(torch, M, stream, a.form)
     cpu = None
     if not a.no_cpu_baseline:
         cores = host_cores()
-        ns = a.cpu_sample or cores
-        r = subprocess.run([sys.executable, os.path.join(HERE, "bench.py"), "--cpu-only", "--workload", a.workload,
-                            "--cpu-sample", str(ns)], capture_output=True, text=True)
-        try:
-            c = json.loads(r.stdout.strip().splitlines()[-1])
-            cpu = {"value": c["value"], "unit": UNIT, "cores": c["cores"], "kind": "port",
-                   "sample": "%d of the workload's nodes, one per process, oracle (C restatement of the reference) "
-                             "in the reference's mode (its rand() streams) with single-threaded OpenBLAS; %.1f s wall"
-                             % (c["nodes"], c["wall"])}
-        except Exception:
-            cpu = {"value": None, "unit": UNIT, "cores": None, "kind": "port", "sample": "failed: " + r.stderr[-300:]}
+        c = cpu_sample(a.workload, a.cpu_sample or cores, cores)
+        cpu = {"value": c["value"], "unit": UNIT, "cores": c["cores"], "kind": "port",
+               "sample": "%d of the workload's nodes, one process per core (started before timing), the oracle "
+                         "(C restatement of the reference) in the reference's mode (its rand() streams) with "
+                         "single-threaded OpenBLAS; %.1f s wall, %.2f s per node" % (c["nodes"], c["wall"],
+                                                                                  c["node_seconds"])}
     admm = sum(s.admm_iters for st in stats for s in st)
     out = {
         "metric": METRIC, "value": total_nodes / dev_s, "unit": UNIT, "n_gpus": world, "steps": a.steps,
         "warmup": a.warmup, "ms_per_step": dev_s * 1e3 / a.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64" if a.form == "fp64" else "bf16 split (FP32-accurate) + f64",
+        "vs_baseline": None, "dtype": DTYPES[a.form],
         "data": "synthetic (seeded rudy-style G(n,p) graph and node fixings)",
-        "config": {"workload": a.workload, "n": wl["n"], "nodes_per_step": batch, "form": a.form,
-                   "projection": FORMS[a.form],
-                   "cuts": "tri+pent" if not wl["params"].get("include_Hepta", 1) else "tri+pent+hept",
-                   "params": "reference shipped params file, " + ", ".join("%s=%s" % kv for kv in wl["params"].items()),
-                   "incumbent": wl["lb"], "l2": "working set per step > L2 (64 nodes x 8 n^2 FP64 buffers)",
-                   "parallelism": "replicas" if world > 1 else "single"},
+        "config": workload_config(wl, world),
+        "form": a.form, "projection": FORMS[a.form],
         "e2e": {"value": total_nodes / wall, "unit": UNIT, "h2d_bytes_per_step": h2d // a.steps,
                 "d2h_bytes_per_step": d2h // a.steps},
         "gpu_launches": launches,
@@ -363,6 +449,7 @@ def run_ours(a):
         "plain_fp64": plain,
         "speedup_vs_plain_fp64": (plain["ms_per_step"] / (dev_s * 1e3 / a.steps)) if plain else None,
         "time_to_optimum": tto,
+        "n512": n512,
         "cpu_baseline": cpu,
         "clocks": clk,
     }
@@ -424,29 +511,59 @@ def cpu_time_to_optimum(cores):
                       "best-first per rank, shared incumbent, queue rebalancing"}
 
 
+def workload_config(wl, world):
+    """The `config` of both arms: the workload only (what is bounded), so that the
+    two lines of one run carry the same config."""
+    return {"workload": wl["name"], "n": wl["n"], "nodes_per_step": len(wl["fixings"]),
+            "cuts": "tri+pent" if not wl["params"].get("include_Hepta", 1) else "tri+pent+hept",
+            "params": "reference shipped params file, " + ", ".join("%s=%s" % kv for kv in wl["params"].items()),
+            "incumbent": wl["lb"], "l2": "working set per step > L2 (64 nodes x 8 n^2 FP64 buffers)",
+            "parallelism": "replicas" if world > 1 else "single"}
+
+
 def run_reference(a):
+    """The reference's method on the host cores: the oracle port in its reference
+    mode, one process per core (created before the timed steps), bounding the
+    workload's nodes.  A timed step bounds `--cpu-sample` nodes (default: all of the
+    step's nodes when that is at most four per core, else one per core), taken in
+    turn from the workload's node list so that successive steps cover all of it;
+    warm-up steps bound one node per core."""
     rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
     if rank != 0:
         return
+    from madam_gb300 import workload as W
+
+    wl = W.make(a.workload)
+    total = len(wl["fixings"])
     cores = host_cores()
-    ns = a.cpu_sample or cores
-    vals = []
-    for i in range(a.warmup + a.steps):
-        r = cpu_sample(a.workload, ns if i >= a.warmup else 1, cores)
-        if i >= a.warmup:
-            vals.append(r)
-    tot_nodes = sum(r["nodes"] for r in vals)
-    tot_wall = sum(r["wall"] for r in vals)
-    v = tot_nodes / tot_wall
+    ns = a.cpu_sample or (total if total <= 4 * cores else cores)
+    pool = CpuPool(a.workload, cores)
+    per_node, walls, done = [], [], 0
+    try:
+        for i in range(a.warmup + a.steps):
+            k = min(cores, total) if i < a.warmup else ns
+            idx = [(done + j) % total for j in range(k)]
+            r = pool.run(idx)
+            if i >= a.warmup:
+                done += k
+                walls.append(r["wall"])
+                per_node += r["node_seconds"]
+    finally:
+        pool.close()
+    tot_wall = sum(walls)
+    v = len(per_node) / tot_wall
+    sample = ("%d of the workload's %d nodes per step (in turn through the node list), one process per core on %d "
+              "cores, each node alone: the oracle (C restatement of the reference, checked bit-for-bit against it) "
+              "in the reference's mode (its rand() streams) with single-threaded OpenBLAS; mean %.2f s per node"
+              % (ns, total, cores, statistics.mean(per_node)))
     out = {
-        "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
-        "steps": a.steps, "warmup": a.warmup, "ms_per_step": tot_wall * 1e3 / a.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
-        "config": {"workload": a.workload, "nodes_per_step": ns},
-        "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": "%d nodes per step, one process per core, oracle (C restatement of the "
-                                   "reference, checked bit-for-bit against it) in the reference's mode (its rand() "
-                                   "streams) with single-threaded OpenBLAS" % ns},
+        "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
+        "ms_per_step": tot_wall * 1e3 / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (seeded rudy-style graph and node fixings)", "impl": "reference",
+        "config": workload_config(wl, world),
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample,
+                         "node_seconds_mean": statistics.mean(per_node)},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     if not a.no_compare:

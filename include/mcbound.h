@@ -157,6 +157,21 @@ int mcb_bound_batch(mcb_ctx *ctx, mcb_bab_node *const *nodes, int count, int ran
  * *nodes counts as the reference does (1 + 2 per branching). */
 int mcb_bab(mcb_ctx *ctx, int batch, int max_nodes, double *opt, int *sol, double *root_bound,
             int *nodes, mcb_node_stats *log, int log_cap, int *log_count);
+/* Iteration cap of the conjugate-gradient solve of (B B^T + I) t = rhs in every ADMM
+ * iteration (default 2000).  The reference factorises B B^T + I with CHOLMOD
+ * (admm.c:480-487,546) and has no such cap; a solve that reaches it before its
+ * tolerance ends that node's bound with MCB_ERR_ITER. */
+int mcb_set_cg_limit(mcb_ctx *ctx, int max_iters);
+/* Wall-time limit of mcb_bab in seconds (0: none), checked before each batch: the
+ * reference's time limit (bab_functions.c:140-147, compiled out there; its report
+ * prints "TIME LIMIT REACHED.", bab_functions.c:360-369).  A run that the node or
+ * time limit stops returns MCB_ERR_CAPACITY with the incumbent in *opt / sol and
+ * mcb_last_error "node limit reached" or "time limit reached". */
+void mcb_set_time_limit(mcb_ctx *ctx, double seconds);
+/* After an mcb_bab run the node or time limit stopped: the largest bound among the
+ * open nodes not pruned by the incumbent (an upper bound on every cut left
+ * unexplored) and their count in *open_nodes; -1e308 and 0 when the tree closed. */
+double mcb_bab_open_bound(const mcb_ctx *ctx, int *open_nodes);
 
 /* ---- operator-level entry points (host pointers; device memory per call) -----
  * Cut arrays: tri = 4 ints per cut (i, j, k, type) with i > j > k (Triangle_Inequality,
@@ -206,6 +221,12 @@ int mcb_autotune_table(const mcb_ctx *ctx, int cap, int *npad, int *bucket, int 
  * loaded entries are used instead of timing. */
 int mcb_autotune_save(const mcb_ctx *ctx, const char *path);
 int mcb_autotune_load(mcb_ctx *ctx, const char *path);
+/* Test of the tensor-core kernel's bounded waits (no counterpart in the reference).
+ * While on (process-wide), the tcgen05 GEMM issues no TMA loads, so nothing is in
+ * flight and its first wait on a full pipeline stage runs out after ~a millisecond:
+ * every call that launches it reports MCB_ERR_ITER, and calls after it is switched
+ * off run normally.  Lets a test drive the expiry path on a GPU without faulting it. */
+void mcb_tc_test_expiry(int on);
 /* largest eigenvalue (admm.c:731-752) and a rigorous upper bound on it */
 int mcb_lambda_max(int n, const double *A, double *lmax, double *lmax_upper);
 /* basic SDP relaxation by the predictor-corrector IPM, ipm_mc_pk.c */

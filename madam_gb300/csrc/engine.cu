@@ -27,6 +27,7 @@
 #include "kernels.h"
 #include "mcb_dev.cuh"
 #include "ns.h"
+#include "tc.h"
 #include "learn.h"
 #include "mlp.h"
 
@@ -158,6 +159,12 @@ struct mcb_ctx {
     long long graph_launches = 0, graph_captures = 0;
     // host-side wall time per phase of bound_batch (seconds)
     double host_s[8] = {};
+    // mcb_bab: wall-time limit (0 = none) and, after a run the node or time limit
+    // stopped, the largest bound among the open nodes and their count
+    int cg_max_iters = 2000;       // CG iterations per solve of (B B^T + I) t = rhs
+    double bab_time_limit = 0.0;
+    double bab_open_bound = -1e308;
+    int bab_open_nodes = 0;
     // instrumentation
     long long h2d = 0, d2h = 0;        // host<->device bytes moved by the bound calls
     long long lib_launches = 0;        // cuBLAS launches (not counted as own kernels)
@@ -433,7 +440,7 @@ int launch_admm_iteration(mcb_ctx *c, int ns, int mmax, int emax) {
         // to rounding); the Newton-Schulz forms carry 1e-7 projection errors, so a
         // 1e-10 solve is still far below anything the ADMM's 1e-3 tolerance sees
         Prof p(c, K_CG, 1);
-        launch_cg(d, ns, 2000, c->proj == MCB_PROJ_FP64 ? 1e-13 : 1e-10, c->st);
+        launch_cg(d, ns, c->cg_max_iters, c->proj == MCB_PROJ_FP64 ? 1e-13 : 1e-10, c->st);
     }
     { Prof p(c, K_SU, 1); launch_admm_su(d, ns, mmax, c->st); }
     { Prof p(c, K_W, 2); launch_build_W(d, ns, N, emax, 0, c->st); }
@@ -462,7 +469,8 @@ int run_chunk(mcb_ctx *c, int ns, int mmax, int emax, int chunk) {
             if (int rc = launch_admm_iteration(c, ns, mmax, emax)) return rc;
         return MCB_OK;
     }
-    std::vector<int> key{ns, mmax, emax, chunk, c->proj, c->ns.npad, c->ns.live, c->ns.variant, c->ns.version};
+    std::vector<int> key{ns, mmax, emax, chunk, c->proj, c->ns.npad, c->ns.live, c->ns.variant, c->ns.version,
+                         c->cg_max_iters, tc_test_expiry()};
     if (!c->gexec || key != c->gkey) {
         long long l0[K_NCLASS];
         double w0[K_NCLASS];
@@ -1362,20 +1370,6 @@ int bound_batch(mcb_ctx *c, mcb_bab_node *const *nodes, int count, int rank, dou
             NodeRun &r = R[si];
             if (want3[si]) r.sep_round++;
             r.done = r.prune || r.giveup || r.status || (r.nbit >= P.ADMM_itermax);
-            if (getenv("MCB_TRACE")) {
-                uint64_t ht = 1, hp = 1, hh = 1;
-                for (int v : r.tri) ht = key2(ht, (uint64_t)v);
-                for (int v : r.pent) hp = key2(hp, (uint64_t)v);
-                for (int v : r.hept) hh = key2(hh, (uint64_t)v);
-                fprintf(stderr, "TRACE round %d nbit %d f %.15g cuts %d %d %d viol3 %.12g viol5 %.12g lb %.1f h %016llx %016llx %016llx\n",
-                        r.count, r.nbit, r.f, (int)r.tri.size() / 4, (int)r.pent.size() / 6, (int)r.hept.size() / 8,
-                        r.viol3, r.viol5, c->LB, (unsigned long long)ht, (unsigned long long)hp, (unsigned long long)hh);
-                if (getenv("MCB_TRACE_SA") && r.count == atoi(getenv("MCB_TRACE_SA"))) {
-                    for (size_t q = 0; q < r.pent.size(); q += 6)
-                        fprintf(stderr, "PENT %d %d %d %d %d %d\n", r.pent[q], r.pent[q + 1], r.pent[q + 2], r.pent[q + 3],
-                                r.pent[q + 4], r.pent[q + 5]);
-                }
-            }
             if ((rc = fetch_lastrow(c, si, r.n, row))) return rc;
             store_fracsol(c, r, row);
         }
@@ -1750,6 +1744,9 @@ int mcb_bab(mcb_ctx *c, int batch, int max_nodes, double *opt, int *sol, double 
             mcb_node_stats *log, int log_cap, int *log_count) {
     if (!c || batch < 1) return MCB_ERR_ARG;
     batch = std::min(batch, c->batch_max);
+    const auto t_start = std::chrono::steady_clock::now();
+    c->bab_open_bound = -1e308;
+    c->bab_open_nodes = 0;
     int lc = 0, nodes = 1, evaluated = 0, rc = MCB_OK;
     Heap h;
     mcb_bab_node *root = (mcb_bab_node *)calloc(1, sizeof(mcb_bab_node));
@@ -1776,6 +1773,12 @@ int mcb_bab(mcb_ctx *c, int batch, int max_nodes, double *opt, int *sol, double 
     std::vector<mcb_node_stats> sts;
     while (rc == MCB_OK && !h.d.empty()) {
         if (max_nodes > 0 && evaluated >= max_nodes) { rc = MCB_ERR_CAPACITY; c->err = "node limit reached"; break; }
+        if (c->bab_time_limit > 0.0 &&
+            std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count() >= c->bab_time_limit) {
+            rc = MCB_ERR_CAPACITY;
+            c->err = "time limit reached";
+            break;
+        }
         cur.clear();
         while (!h.d.empty() && (int)cur.size() < batch) cur.push_back(h.pop());
         b.assign(cur.size(), 0);
@@ -1805,7 +1808,14 @@ int mcb_bab(mcb_ctx *c, int batch, int max_nodes, double *opt, int *sol, double 
             free(cur[a]);
         }
     }
-    for (auto *n : h.d) free(n);
+    // the open nodes' bounds (their parents' bounds) bound every cut still unexplored
+    for (auto *n : h.d) {
+        if (c->LB + 1.0 < n->upper_bound) {
+            c->bab_open_bound = std::max(c->bab_open_bound, n->upper_bound);
+            c->bab_open_nodes++;
+        }
+        free(n);
+    }
     c->warm_in.clear();
     if (opt) *opt = c->LB;
     if (sol) memcpy(sol, c->best_sol.data(), c->pb * sizeof(int));
@@ -1843,6 +1853,18 @@ int mcb_host_stats(const mcb_ctx *c, int cap, char (*names)[32], double *seconds
 void mcb_graph_stats(const mcb_ctx *c, long long *captures, long long *replays) {
     if (captures) *captures = c ? c->graph_captures : 0;
     if (replays) *replays = c ? c->graph_launches : 0;
+}
+int mcb_set_cg_limit(mcb_ctx *c, int max_iters) {
+    if (!c || max_iters < 1) return MCB_ERR_ARG;
+    c->cg_max_iters = max_iters;
+    return MCB_OK;
+}
+void mcb_set_time_limit(mcb_ctx *c, double seconds) {
+    if (c) c->bab_time_limit = seconds > 0.0 ? seconds : 0.0;
+}
+double mcb_bab_open_bound(const mcb_ctx *c, int *open_nodes) {
+    if (open_nodes) *open_nodes = c ? c->bab_open_nodes : 0;
+    return c ? c->bab_open_bound : -1e308;
 }
 void mcb_set_profile(mcb_ctx *c, int on) {
     if (!c) return;

@@ -248,6 +248,7 @@ __global__ void __launch_bounds__(512) k_admm_finish(Slot *slots, double scaleSi
         else if (dd - dp > 0.5) s.sigma *= scaleSigma;
         if (err < s.tol || s.nbit > itermax) s.stop = 1;
         if (!(err == err)) { s.stop = 1; s.status = -4; }
+        if (s.status) s.stop = 1;  // a failed step (e.g. the CG cap) ends this node's ADMM
     }
 }
 

@@ -96,6 +96,11 @@ __global__ void k_ipm_init(Slot *slots) {
         s.acc[ACC_IPM_IT] = 0;
         s.acc[ACC_IPM_INFO] = 0;
         s.acc[ACC_IPM_DONE] = (py - pl > 1e-4) ? 0.0 : 1.0;
+        // a non-finite objective (NaN or overflow in L) cannot start the IPM
+        if (!isfinite(py) || !isfinite(pl)) {
+            s.acc[ACC_IPM_DONE] = 1.0;
+            s.status = -4;
+        }
     }
 }
 

@@ -28,8 +28,7 @@
 // global store is coalesced and 64 or 128 bits wide.  Every wait on an
 // mbarrier is bounded: on expiry the CTA records an error code, gives the TMA
 // loads it still has in flight their own bounded wait, skips the rest and
-// releases its tensor memory.  Compiled with MCB_TC_TRACE, CTA (0, 0) records
-// globaltimer stamps of its phases (read by mcb_tc_trace) for latency studies.
+// releases its tensor memory.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -55,6 +54,10 @@ constexpr int kStageBytes = 2 * kPieces * kTileBytes;    // A and B, three piece
 constexpr int smem_bytes(int stages) { return stages * kStageBytes + 1024 + 128; }
 constexpr uint32_t kTmemCols = 256;  // two 128-column FP32 accumulators: hi.hi, and the corrections
 constexpr long long kSpinLimit = 1ll << 26;  // bounded waits (~a second)
+// the expiry test: no TMA loads are issued (nothing is ever in flight), so the
+// first wait on a full stage runs out after this many polls (~a millisecond)
+constexpr long long kTestSpinLimit = 1ll << 16;
+std::atomic<int> g_test_expiry{0};
 
 // the six piece products (A piece, B piece)
 __constant__ int kProdA[6] = {0, 0, 1, 1, 0, 2};
@@ -68,9 +71,9 @@ __device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
 __device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
 }
-// true when the phase with the given parity has completed; false after the spin limit
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
-    for (long long it = 0; it < kSpinLimit; ++it) {
+// true when the phase with the given parity has completed; false after `limit` polls
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, long long limit) {
+    for (long long it = 0; it < limit; ++it) {
         uint32_t done;
         asm volatile(
             "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
@@ -158,23 +161,11 @@ struct Maps {
     CUtensorMap a[kPieces], b[kPieces];
 };
 
-#ifdef MCB_TC_TRACE
-__device__ unsigned long long g_tc_trace[64];
-__device__ __forceinline__ void trace(int k) {
-    if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) {
-        unsigned long long t;
-        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-        g_tc_trace[k] = t;
-    }
-}
-#else
-__device__ __forceinline__ void trace(int) {}
-#endif
 
 template <int kStages>
 __global__ void __launch_bounds__(128, 3 - kStages) k_tc_gemm(const __grid_constant__ Maps maps, TcOut out, int npad,
                                                    const int *live, const int *nlist, float alpha, float diag,
-                                                   int sym) {
+                                                   int sym, long long spin_limit, int issue_loads) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint64_t *full = (uint64_t *)(smem + kStages * kStageBytes);
@@ -194,7 +185,6 @@ __global__ void __launch_bounds__(128, 3 - kStages) k_tc_gemm(const __grid_const
     const int m0 = ti * BM, n0 = tj * BN;
     const int slot = live[blockIdx.y];
     const int nk = npad / BK;
-    trace(0);
 
     if (tid == 0) {
         for (int s = 0; s < kStages; ++s) {
@@ -214,12 +204,12 @@ __global__ void __launch_bounds__(128, 3 - kStages) k_tc_gemm(const __grid_const
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = *tmem_slot;
-    trace(1);
 
     if (tid == 0) {
         const uint32_t idesc = instr_desc(BM, BN);
         int issued = 0, landed = 0;  // chunks whose loads were issued / have been waited for
         auto load = [&](int kc) {
+            if (!issue_loads) return;  // the expiry test: nothing is issued, nothing is in flight
             const int s = kc % kStages;
             unsigned char *st = smem + s * kStageBytes;
             mbar_expect_tx(&full[s], kStageBytes);
@@ -234,10 +224,9 @@ __global__ void __launch_bounds__(128, 3 - kStages) k_tc_gemm(const __grid_const
         for (int kc = 0; kc < nk && ok; ++kc) {
             const int s = kc % kStages;
             const uint32_t use = (uint32_t)(kc / kStages) & 1u;
-            ok = mbar_wait(&full[s], use);
+            ok = mbar_wait(&full[s], use, spin_limit);
             if (!ok) break;
             ++landed;
-            trace(2 + 2 * kc);
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             const uint32_t base = smem_u32(smem + s * kStageBytes);
 #pragma unroll
@@ -255,9 +244,8 @@ __global__ void __launch_bounds__(128, 3 - kStages) k_tc_gemm(const __grid_const
             mma_commit(&empty[s]);
             // refill this stage once its MMAs have read it
             if (kc + kStages < nk) {
-                ok = mbar_wait(&empty[s], use);
+                ok = mbar_wait(&empty[s], use, spin_limit);
                 if (!ok) break;
-                trace(3 + 2 * kc);
                 load(kc + kStages);
             }
         }
@@ -265,16 +253,15 @@ __global__ void __launch_bounds__(128, 3 - kStages) k_tc_gemm(const __grid_const
             s_fail = 1;
             // loads still in flight write this CTA's shared memory: give them their
             // own bounded wait before the block can exit and the memory is reused
-            for (int j = landed; j < issued; ++j) mbar_wait(&full[j % kStages], (uint32_t)(j / kStages) & 1u);
+            for (int j = landed; j < issued; ++j) mbar_wait(&full[j % kStages], (uint32_t)(j / kStages) & 1u, kSpinLimit);
         }
         mma_commit(done);
     }
     __syncwarp();
     // every thread waits for the accumulator; the outcome is made block-uniform
-    bool ok = mbar_wait(done, 0);
+    bool ok = mbar_wait(done, 0, kSpinLimit);
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const int bad = __syncthreads_or(!ok || s_fail);
-    trace(40);
     if (bad) {
         if (tid == 0 && out.err) atomicExch(out.err, MCB_ERR_ITER);
     } else {
@@ -342,7 +329,6 @@ __global__ void __launch_bounds__(128, 3 - kStages) k_tc_gemm(const __grid_const
             }
         }
         __syncthreads();
-        trace(42);
         // direct half: warp per row, lane per 4 columns; diagonal tiles keep col <= row
         for (int rr = warp; rr < BM; rr += 4) {
             const int c = 4 * lane;
@@ -351,7 +337,6 @@ __global__ void __launch_bounds__(128, 3 - kStages) k_tc_gemm(const __grid_const
             // on a diagonal tile, columns c .. min(c + 3, rr)
             store4(sb + (size_t)(m0 + rr) * npad + n0 + c, x, 0, diag_tile ? min(3, rr - c) : 3);
         }
-        trace(43);
         if (sym) {
             __syncthreads();
             // (2) column-major tile F[c][r] = C(m0 + r, n0 + c), from the accumulators again
@@ -363,7 +348,6 @@ __global__ void __launch_bounds__(128, 3 - kStages) k_tc_gemm(const __grid_const
                 for (int j = 0; j < 32; ++j) F[(c0 + j) * LD + r] = value(v[j] + w[j], m0 + r, n0 + c0 + j);
             }
             __syncthreads();
-            trace(44);
             // mirrored half: output row n0 + cc, lane per 4 rows of the tile; diagonal
             // tiles keep rows strictly below the diagonal (rr > cc)
             for (int cc = warp; cc < BN; cc += 4) {
@@ -375,7 +359,6 @@ __global__ void __launch_bounds__(128, 3 - kStages) k_tc_gemm(const __grid_const
             }
         }
     }
-    trace(41);
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     if (warp == 0)
@@ -460,12 +443,16 @@ int tc_gemm(const void *amaps, const void *bmaps, const TcOut &out, int npad, in
     memcpy(m.b, bmaps, sizeof(m.b));
     const int nt = npad / BM;
     dim3 grid(sym ? nt * (nt + 1) / 2 : nt * nt, nlive);
+    const int test = g_test_expiry.load();
+    const long long spins = test ? kTestSpinLimit : kSpinLimit;
     if (variant == 0)
-        k_tc_gemm<1><<<grid, 128, smem_bytes(1), st>>>(m, out, npad, d_live, d_n, alpha, diag, sym);
+        k_tc_gemm<1><<<grid, 128, smem_bytes(1), st>>>(m, out, npad, d_live, d_n, alpha, diag, sym, spins, !test);
     else
-        k_tc_gemm<2><<<grid, 128, smem_bytes(2), st>>>(m, out, npad, d_live, d_n, alpha, diag, sym);
+        k_tc_gemm<2><<<grid, 128, smem_bytes(2), st>>>(m, out, npad, d_live, d_n, alpha, diag, sym, spins, !test);
     return cudaGetLastError() == cudaSuccess ? MCB_OK : MCB_ERR_CUDA;
 }
+
+int tc_test_expiry() { return g_test_expiry.load(); }
 
 void tc_split_f32(const float *src, size_t sstride, const TcOut &out, int npad, int nlive, const int *d_live,
                   cudaStream_t st) {
@@ -482,10 +469,8 @@ void tc_split_f64(const double *src, size_t sstride, const TcOut &out, int npad,
     k_tc_split<double><<<dim3(g, nlive), 256, 0, st>>>(src, sstride, out, npad, d_live);
 }
 
-#ifdef MCB_TC_TRACE
-extern "C" int mcb_tc_trace(unsigned long long *out) {
-    return cudaMemcpyFromSymbol(out, g_tc_trace, sizeof(g_tc_trace)) == cudaSuccess ? 0 : -2;
-}
-#endif
 
 }  // namespace mcb
+
+// The expiry test of the bounded waits (see mcbound.h).
+extern "C" void mcb_tc_test_expiry(int on) { mcb::g_test_expiry.store(on ? 1 : 0); }

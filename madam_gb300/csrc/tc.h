@@ -27,6 +27,8 @@ int tc_make_map(void *map, const __nv_bfloat16 *base, int npad, size_t stride, i
 constexpr int kTcVariants = 2;
 int tc_gemm(const void *amaps, const void *bmaps, const TcOut &out, int npad, int nlive, const int *d_live,
             const int *d_n, float alpha, float diag, cudaStream_t st, int sym, int variant);
+// 1 while the expiry test of the bounded waits is on (mcb_tc_test_expiry)
+int tc_test_expiry();
 // three BF16 pieces of FP32 / FP64 matrices (row-major, source slots `sstride` apart)
 void tc_split_f32(const float *src, size_t sstride, const TcOut &out, int npad, int nlive, const int *d_live,
                   cudaStream_t st);

@@ -88,7 +88,11 @@ def node(fixed=None):
 
 
 class MCBError(RuntimeError):
-    pass
+    """A non-zero status of the library; `code` is the MCB_ERR_* value."""
+
+    def __init__(self, msg, code=None):
+        super().__init__(msg)
+        self.code = code
 
 
 _lib = None
@@ -122,6 +126,12 @@ def lib():
     L.mcb_bound_batch.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p]
     L.mcb_bab.argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_double), C.c_void_p, C.POINTER(C.c_double),
                           C.POINTER(C.c_int), C.c_void_p, C.c_int, C.POINTER(C.c_int)]
+    L.mcb_set_time_limit.argtypes = [C.c_void_p, C.c_double]
+    L.mcb_set_cg_limit.argtypes = [C.c_void_p, C.c_int]
+    L.mcb_tc_test_expiry.argtypes = [C.c_int]
+    L.mcb_tc_test_expiry.restype = None
+    L.mcb_bab_open_bound.restype = C.c_double
+    L.mcb_bab_open_bound.argtypes = [C.c_void_p, C.POINTER(C.c_int)]
     L.mcb_op_B.argtypes = [C.c_int, _dp, C.c_int, _ip, C.c_int, _ip, C.c_int, _ip, _dp]
     L.mcb_op_Bt.argtypes = [C.c_int, _dp, C.c_int, _ip, C.c_int, _ip, C.c_int, _ip, _dp]
     L.mcb_project_psd.argtypes = [C.c_int, _dp, C.c_int, _dp, _dp, _dp, _dp, C.POINTER(C.c_int)]
@@ -178,7 +188,7 @@ def _check(rc, ctx=None):
             extra = lib().mcb_last_error(ctx).decode()
             if extra:
                 msg += ": " + extra
-        raise MCBError("mcbound error %d (%s)" % (rc, msg))
+        raise MCBError("mcbound error %d (%s)" % (rc, msg), rc)
 
 
 class Context:
@@ -249,13 +259,25 @@ class Context:
         log = (NodeStats * log_cap)()
         rc = lib().mcb_bab(self.h, batch, max_nodes, C.byref(opt), sol.ctypes.data, C.byref(rb), C.byref(nodes),
                            C.cast(log, C.c_void_p), log_cap, C.byref(lc))
-        # the node limit ends the search early with the incumbent so far, as the
-        # reference's time limit does (bab_functions.c:360-369): not an error
-        stopped = rc == ERR_CAPACITY and max_nodes > 0 and lib().mcb_last_error(self.h) == b"node limit reached"
+        # the node or time limit ends the search early with the incumbent so far, as
+        # the reference's time limit does (bab_functions.c:360-369): not an error
+        stopped = rc == ERR_CAPACITY and lib().mcb_last_error(self.h) in (b"node limit reached",
+                                                                           b"time limit reached")
         if not stopped:
             _check(rc, self.h)
+        on = C.c_int()
+        ob = lib().mcb_bab_open_bound(self.h, C.byref(on))
         return dict(nodes=nodes.value, opt=opt.value, sol=sol[: self.N - 1].copy(), root_bound=rb.value,
-                    log=[log[i] for i in range(lc.value)], stopped=stopped)
+                    log=[log[i] for i in range(lc.value)], stopped=stopped,
+                    open_bound=ob if on.value else None, open_nodes=on.value)
+
+    def set_cg_limit(self, max_iters):
+        """Iteration cap of the CG solve in every ADMM iteration (default 2000)."""
+        _check(lib().mcb_set_cg_limit(self.h, int(max_iters)), self.h)
+
+    def set_time_limit(self, seconds):
+        """Wall-time limit of bab() (0: none)."""
+        lib().mcb_set_time_limit(self.h, float(seconds))
 
     def kernel_stats(self):
         cap = 64
@@ -397,6 +419,11 @@ class MLP:
         _check(lib().mcb_mlp_train(self.h, X.ctypes.data, Y.ctypes.data, len(X), epochs, batch, lr, seed,
                                    C.byref(loss)))
         return float(loss.value)
+
+
+def tc_test_expiry(on):
+    """Switch the tensor-core kernel's wait-expiry test on or off (process-wide)."""
+    lib().mcb_tc_test_expiry(1 if on else 0)
 
 
 def fp64_peak_gflops():

@@ -66,7 +66,13 @@ def balance_plan(sizes):
 def sharded_bab(ctx, new_node, dist=None, depth=2, max_nodes=100000, balance=True, info=None, batch=1,
                 root_only=False, strategy=1):
     """Returns (optimum, solution vector, nodes evaluated on this rank, evaluated on all ranks).
-    info (a dict, optional) receives the number of rebalancing transfers and nodes moved.
+    Every rank returns the same solution: the vector of the lowest rank whose own
+    search found a cut of the optimum's value.  The node total counts the top of the
+    tree, which every rank bounds, once.  max_nodes caps the nodes a rank bounds
+    after the top of the tree; once any rank reaches it, all ranks stop in the same
+    round (the decision is itself a reduction, so the collectives stay matched).
+    info (a dict, optional) receives the number of rebalancing transfers and nodes moved,
+    the nodes this rank bounded after the top of the tree, and the top's node count.
     root_only: bound the root and stop (the reference's `root` parameter, main.c:106,195).
     strategy: the reference's branchingStrategy (1 most fractional, 0 least fractional;
     getBranchingVariable, bab_functions.c:389-423)."""
@@ -120,6 +126,7 @@ def sharded_bab(ctx, new_node, dist=None, depth=2, max_nodes=100000, balance=Tru
             nxt += children(cb, fx, nd)
         frontier = nxt
     lb, sol = ctx.lb()
+    sol_val = lb  # the value of this rank's own best solution `sol`
     # deal the frontier; each rank keeps a best-first heap keyed on the bound
     mine = [f for k, f in enumerate(sorted(frontier, key=lambda t: sorted(t[1].items()))) if k % world == rank]
     tie = itertools.count()
@@ -133,7 +140,9 @@ def sharded_bab(ctx, new_node, dist=None, depth=2, max_nodes=100000, balance=Tru
             lb = g
             ctx.set_lb(lb, None)
         active = allreduce(float(len(heap)), SUM)
-        if active == 0 or local >= max_nodes:
+        # every rank leaves in the same round: the cap is tested collectively
+        capped = allreduce(float(local >= max_nodes), MAX)
+        if active == 0 or capped > 0:
             break
         if dist and balance and world > 1:
             sizes = [None] * world
@@ -168,7 +177,7 @@ def sharded_bab(ctx, new_node, dist=None, depth=2, max_nodes=100000, balance=Tru
             local += len(take)
             lb2, sol2 = ctx.lb()
             if lb2 > lb:
-                lb, sol = lb2, sol2
+                lb, sol, sol_val = lb2, sol2, lb2
             for (fx, nd), b in zip(take, bounds):
                 if lb + 1.0 < b:
                     ic = _branch_var(nd, pb, strategy)
@@ -179,8 +188,15 @@ def sharded_bab(ctx, new_node, dist=None, depth=2, max_nodes=100000, balance=Tru
                         f2[ic] = v
                         heapq.heappush(heap, (-b, next(tie), f2, new_node(f2)))
     best = allreduce(lb, MAX)
-    total = allreduce(float(local + evaluated), SUM)
+    # the top of the tree was bounded identically on every rank: count it once
+    total = allreduce(float(local), SUM) + evaluated
     if info is not None:
-        info.update(transfers=transfers, moved=moved)
-    own = np.asarray(sol)[:pb] if lb == best else None
+        info.update(transfers=transfers, moved=moved, local=local, top=evaluated)
+    own = np.asarray(sol, dtype=np.int32)[:pb] if sol is not None else None
+    if dist and world > 1:
+        # the lowest rank whose own solution attains the optimum hands it to all
+        winner = int(allreduce(float(rank if (own is not None and sol_val == best) else world), dist.ReduceOp.MIN))
+        got = [own if rank == winner else None]
+        dist.broadcast_object_list(got, src=min(winner, world - 1))
+        own = got[0]
     return best, own, local + evaluated, int(total)

@@ -13,7 +13,9 @@ import pytest
 from madam_gb300 import graphs as G
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = "/root/reference"
+from oracle.refdir import reference_dir
+
+REF = reference_dir() or os.path.join(os.sep, "nonexistent-reference")
 
 
 def test_extended_laplacian_matches_oracle(orc):
@@ -289,7 +291,7 @@ class _BatchedOracle:
         return self.c.lb()
 
 
-def _sharded_worker(rank, world, port, q, depth=2, batch=1):
+def _sharded_worker(rank, world, port, q, depth=2, batch=1, max_nodes=100000):
     import torch.distributed as dist
 
     os.environ["MASTER_ADDR"] = "127.0.0.1"
@@ -307,7 +309,7 @@ def _sharded_worker(rank, world, port, q, depth=2, batch=1):
         ctx = _BatchedOracle(ctx)
     info = {}
     best, sol, mine, total = sharded_bab(ctx, lambda fx: O.make_node(n - 1, fx), dist=dist, depth=depth, info=info,
-                                         batch=batch)
+                                         batch=batch, max_nodes=max_nodes)
     if batch > 1:
         info["batch_sizes"] = ctx.sizes
     q.put((rank, best, mine, total, None if sol is None else G2.cut_value(n, e, w, sol), info))
@@ -337,13 +339,39 @@ def test_sharded_branch_and_bound_on_gloo_ranks(orc, world, depth, batch):
     serial = c.bab(max_nodes=5000)
     bests = {r[1] for r in res}
     assert bests == {serial["opt"]}
-    assert any(r[4] == serial["opt"] for r in res)
+    # every rank returns a solution of the optimum's value (the winner's vector)
+    assert all(r[4] == serial["opt"] for r in res)
     assert len({r[3] for r in res}) == 1
+    # the top of the tree, bounded identically on every rank, is counted once
+    assert len({r[5]["top"] for r in res}) == 1
+    assert res[0][3] == sum(r[5]["local"] for r in res) + res[0][5]["top"]
     if world == 3:  # one of three ranks starts with an empty queue (a frontier of two nodes)
         assert res[0][5]["transfers"] >= 1 and res[0][5]["moved"] >= 1
     if batch > 1:
         sizes = [k for r in res for k in r[5]["batch_sizes"]]
         assert sizes and max(sizes) <= batch and max(sizes) > 1
+
+
+def test_sharded_node_cap_stops_every_rank_in_the_same_round(orc):
+    """A node cap that one rank reaches before the others: all ranks leave the
+    loop together (no unmatched collective), agree on the incumbent, and each
+    returns a solution that attains it."""
+    import torch.multiprocessing as mp
+
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = 29500 + (os.getpid() + 911) % 1000
+    ps = [ctx.Process(target=_sharded_worker, args=(r, 2, port, q, 2, 1, 3)) for r in range(2)]
+    for p in ps:
+        p.start()
+    res = [q.get(timeout=600) for _ in ps]
+    for p in ps:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    assert len({r[1] for r in res}) == 1
+    assert all(r[4] == r[1] for r in res)
+    assert max(r[5]["local"] for r in res) <= 3 + 1
+    assert min(r[5]["local"] for r in res) < 5
 
 
 def test_sharded_root_only(orc):
@@ -497,7 +525,7 @@ def test_solve_reads_parameter_files(tmp_path):
     p.write_text("scaleSigma=1.002\n  unknown_name = 7\nTriIneq = 1e-4\nsigma0 = 1.6abc\nminTol\t= 9\n")
     v2 = S.read_params(str(p))
     assert v2["scaleSigma"] == 7.0 and v2["TriIneq"] == 1 and v2["sigma0"] == 1.6 and v2["minTol"] == 1e-4
-    ref = "/root/reference/params"
+    ref = os.path.join(REF, "params")
     if os.path.exists(ref):
         assert S.read_params(ref) == {k: type(M.SHIPPED[k])(v) for k, v in M.SHIPPED.items()}
     # the report parses like the reference's .output files
@@ -518,19 +546,19 @@ def test_solve_reads_parameter_files(tmp_path):
     assert "Maximum value" not in stop
 
 
-@pytest.mark.skipif(not os.path.isdir("/root/reference"), reason="reference headers not present")
+@pytest.mark.skipif(not os.path.isdir(REF), reason="reference headers not present")
 def test_reference_shim_compiles_against_the_reference_headers():
     """The C binding a maintainer adds to MADAM (madam_gb300/shim) compiles against
     the reference's admm.h (with the oracle's single-rank mpi.h) and mcbound.h."""
     root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-    r = subprocess.run(["gcc", "-std=gnu11", "-Wall", "-Werror", "-fsyntax-only", "-I/root/reference",
+    r = subprocess.run(["gcc", "-std=gnu11", "-Wall", "-Werror", "-fsyntax-only", "-I" + REF,
                         "-I" + os.path.join(root, "oracle", "ref"), "-I" + os.path.join(root, "include"),
                         os.path.join(root, "madam_gb300", "shim", "mcb_madam_shim.c")],
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
 
 
-@pytest.mark.skipif(not os.path.isdir("/root/reference"), reason="reference sources not present")
+@pytest.mark.skipif(not os.path.isdir(REF), reason="reference sources not present")
 def test_reference_driver_links_against_the_library(tmp_path):
     """The reference's own driver, heap, input and heuristic files, linked with the
     shim in place of the bound files and with libmcbound, resolve every symbol.
@@ -542,7 +570,7 @@ def test_reference_driver_links_against_the_library(tmp_path):
 
     B.build()
     root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-    mk = subprocess.run(["make", "-s", "-C", os.path.join(root, "oracle", "ref"), "REFDIR=/root/reference",
+    mk = subprocess.run(["make", "-s", "-C", os.path.join(root, "oracle", "ref"), "REFDIR=" + REF,
                          "LAPACK=" + OB.find_lapack(), "../_ref/madam_drop_in"], capture_output=True, text=True)
     assert mk.returncode == 0, mk.stderr[-2000:]
     n, e, w = G.gnp(40, 0.5, "one", seed=1)  # the reference fixture gnp40_one_s1 (optimum 246)

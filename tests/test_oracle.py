@@ -13,7 +13,9 @@ import pytest
 from madam_gb300 import graphs as G
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = "/root/reference"
+from oracle.refdir import reference_dir
+
+REF = reference_dir() or os.path.join(os.sep, "nonexistent-reference")
 
 
 def test_glibc_rand_restatement_matches_libc(orc):

@@ -7,17 +7,21 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def _sym(n, seed):
+def _sym(n, seed, sign=0.0):
     A = np.random.default_rng(seed).standard_normal((n, n))
+    if n == 1:  # a 1 x 1 matrix of the given sign
+        return np.array([[sign * (1.0 + abs(A[0, 0]))]])
     return 1.5 * (A + A.T)
 
 
 def test_noalloc_projection_matches_allocating_entry_point(gpu_lib):
     torch = pytest.importorskip("torch")
     stream = torch.cuda.current_stream().cuda_stream
-    # two calls in a row, the second smaller, so stale scratch from the first would show
-    for n, seed in ((300, 11), (97, 12)):
-        W = _sym(n, seed)
+    # calls in a row that share the scratch: its largest size (n = 512 fills it),
+    # then smaller ones, so stale scratch from an earlier call would show, down to
+    # the 1 x 1 matrices (one positive eigenvalue, then none)
+    for n, seed, sign in ((512, 10, 0.0), (300, 11, 0.0), (97, 12, 0.0), (1, 13, 1.0), (1, 14, -1.0)):
+        W = _sym(n, seed, sign)
         Xp, Q, Z, ev = gpu_lib.project(W)
         dW = torch.tensor(W.ravel(order="F"), dtype=torch.float64, device="cuda")
         dXp = torch.full((n * n,), np.nan, dtype=torch.float64, device="cuda")
@@ -28,6 +32,8 @@ def test_noalloc_projection_matches_allocating_entry_point(gpu_lib):
                                     stream=stream)
         torch.cuda.synchronize()
         assert M == len(ev)
+        if n == 1:
+            assert M == (1 if sign > 0 else 0)
         scale = max(1.0, np.abs(W).max())
         Xn = dXp.cpu().numpy().reshape(n, n, order="F")
         Qn = dQ.cpu().numpy().reshape(n, n, order="F")
