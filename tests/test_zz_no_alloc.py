@@ -41,8 +41,9 @@ def test_noalloc_projection_matches_allocating_entry_point(gpu_lib):
         assert np.abs(Xn - Xp).max() <= 1e-10 * scale * n
         assert np.abs(np.tril(Qn) - np.tril(Q)).max() <= 1e-10 * scale * n
         assert np.all(np.triu(Qn, 1) == 0.0)
-        assert np.abs(Zn - Z).max() <= 1e-8 * scale
-        assert np.abs(dev.cpu().numpy()[:M] - ev).max() <= 1e-11 * scale
+        if M > 0:  # no factor and no eigenvalues to compare when nothing is positive
+            assert np.abs(Zn - Z).max() <= 1e-8 * scale
+            assert np.abs(dev.cpu().numpy()[:M] - ev).max() <= 1e-11 * scale
 
 
 def test_noalloc_rejects_sizes_beyond_its_scratch(gpu_lib):
