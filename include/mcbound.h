@@ -47,14 +47,15 @@ enum mcb_status {
 /* Projection forms (mcb_create flags, low byte) */
 #define MCB_PROJ_FP64 0x0      /* plain: FP64 tridiagonal eigensolver (dsyevr's method) */
 #define MCB_PROJ_NS_BF16 0x1   /* chosen: Newton-Schulz sign iteration on the tensor cores (tcgen05, operands
-                                  as three BF16 pieces: FP32-accurate), FP64 assembly and safe bound */
+                                  as five BF16 digit planes: ~5e-10 per product), FP64 assembly and safe bound */
 #define MCB_PROJ_NS_TF32 0x2   /* chosen: as MCB_PROJ_NS_BF16; with MCB_NS_OPERANDS_NATIVE its one-pass
                                   steps use TF32 operands (cuBLAS) instead of BF16 */
 /* Other flags */
 #define MCB_FLAG_PROFILE 0x100 /* time every kernel class with CUDA events */
 /* operands of the Newton-Schulz growth steps (mcb_ns_options) */
 #define MCB_NS_OPERANDS_NATIVE 0 /* one pass of the form's type (BF16 / TF32): rounding floor ~1e-3 */
-#define MCB_NS_OPERANDS_SPLIT 1  /* FP32-accurate: three BF16 pieces per operand, own tcgen05 kernel (default) */
+#define MCB_NS_OPERANDS_SPLIT 1  /* five BF16 digit planes per operand, exact digit-sum groups, own tcgen05
+                                    kernel (default) */
 #define MCB_NS_OPERANDS_FP32 2   /* FP32 FMA through cuBLAS, no tensor cores (reference point) */
 #define MCB_NS_OPERANDS_CUBLAS_SPLIT 3 /* cuBLAS's BF16x9 emulation of FP32 (reference point) */
 #define MCB_FLAG_LEARNED 0x200 /* learned cut ranking + dual warm start (models set by mcb_set_models) */
@@ -206,11 +207,13 @@ int mcb_project_psd_noalloc(int n, const double *W, double *Xp, double *Q, doubl
                             void *stream);
 /* The tensor-core GEMM of the Newton-Schulz form (no counterpart in the
  * reference): C = alpha A B^T + diag I for `batch` row-major npad x npad FP32
- * matrices (host buffers), each operand split into three BF16 pieces, six piece
- * products accumulated in FP32 by tcgen05.mma.  npad a multiple of 128, <= 1024.
- * sym = 1 computes the lower 128 x 128 tiles only and mirrors them (for products
- * known to be symmetric).  variant: 0 = one pipeline stage, two CTAs per SM;
- * 1 = two stages, one CTA per SM (the autotuner picks per matrix order). */
+ * matrices (host buffers).  Each operand is scaled by a power of two and cut into
+ * five signed 7-bit digits, one BF16 plane each; tcgen05.mma sums the nineteen
+ * plane products of digit sum <= 5 in four FP32 accumulators, the three leading
+ * digit-sum groups exactly, so C is accurate to ~5e-10 of its norm before its
+ * rounding to FP32.  npad a multiple of 128, <= 1024.  sym = 1 computes the lower
+ * 128 x 128 tiles only and mirrors them (for products known to be symmetric).
+ * variant: 0 = two pipeline stages, 1 = one (the autotuner picks per matrix order). */
 int mcb_split_gemm(int npad, int batch, const float *A, const float *B, float alpha, float diag, int sym,
                    int variant, float *C);
 /* The autotuner's table of a context (Newton-Schulz forms): for every (npad,

@@ -403,8 +403,8 @@ int launch_ns_projection(mcb_ctx *c, int ns) {
     Slot *d = c->d_slots;
     NsProj &P = c->ns;
     {
-        Prof p(c, K_NSPREP, P.tc() ? 4 : 2);
-        launch_ns_prep(d, ns, P.npad, P.stride, P.S, P.Wd, 1, c->st);
+        Prof p(c, K_NSPREP, P.tc() ? 3 : 2);
+        launch_ns_prep(d, ns, P.npad, P.stride, P.S, P.Wd, P.d_alpha, 1, c->st);
         if (P.tc()) P.split_inputs(c->st);
     }
     double lo = P.flops_lo, hi = P.flops_hi, f64 = P.flops_fp64;

@@ -19,7 +19,7 @@ namespace {
 constexpr int TT = 32;  // tile edge of the copy kernels
 
 // ||W||_F from the lower triangle (an upper bound on the spectral radius)
-__global__ void __launch_bounds__(512) k_ns_alpha(Slot *slots, int gate) {
+__global__ void __launch_bounds__(512) k_ns_alpha(Slot *slots, double *alpha_out, int gate) {
     Slot &s = slots[blockIdx.x];
     if (!gated(s, gate)) return;
     const int n = s.n;
@@ -33,7 +33,10 @@ __global__ void __launch_bounds__(512) k_ns_alpha(Slot *slots, int gate) {
         }
     }
     a = block_sum(a, red);
-    if (threadIdx.x == 0) s.acc[ACC_NS_ALPHA] = sqrt(a);
+    if (threadIdx.x == 0) {
+        s.acc[ACC_NS_ALPHA] = sqrt(a);
+        if (alpha_out) alpha_out[blockIdx.x] = sqrt(a);
+    }
 }
 
 // Wd = W (full, FP64, padded to npad with zeros), S = W / alpha (FP32).
@@ -269,8 +272,9 @@ inline int grid_for(size_t tot) {
 
 }  // namespace
 
-void launch_ns_prep(Slot *d, int ns, int npad, size_t stride, float *S, double *Wd, int gate, cudaStream_t st) {
-    k_ns_alpha<<<ns, 512, 0, st>>>(d, gate);
+void launch_ns_prep(Slot *d, int ns, int npad, size_t stride, float *S, double *Wd, double *alpha_out, int gate,
+                    cudaStream_t st) {
+    k_ns_alpha<<<ns, 512, 0, st>>>(d, alpha_out, gate);
     int nt = (npad + TT - 1) / TT;
     k_ns_scale<<<dim3(nt * nt, ns), 256, 0, st>>>(d, npad, stride, S, Wd, gate);
 }
@@ -366,13 +370,14 @@ int NsProj::init(int form_, int nmax_, int cap_, cudaStream_t st) {
     if (cudaMalloc(&Gd, tot * sizeof(double)) != cudaSuccess) return MCB_ERR_NOMEM;
     if (cudaMalloc(&dptr, 6 * (size_t)cap * sizeof(void *)) != cudaSuccess) return MCB_ERR_NOMEM;
     hptr.assign(6 * (size_t)cap, nullptr);
-    for (__nv_bfloat16 **b : {&Sp, &S2p, &Tp, &Wp})
-        if (cudaMalloc(b, 3 * tot * sizeof(__nv_bfloat16)) != cudaSuccess) return MCB_ERR_NOMEM;
+    for (__nv_bfloat16 **b : {&Wp, &Sp, &S2p, &Tp})
+        if (cudaMalloc(b, kTcPieces * tot * sizeof(__nv_bfloat16)) != cudaSuccess) return MCB_ERR_NOMEM;
+    if (cudaMalloc(&d_alpha, cap * sizeof(double)) != cudaSuccess) return MCB_ERR_NOMEM;
     if (cudaMalloc(&d_live, cap * sizeof(int)) != cudaSuccess) return MCB_ERR_NOMEM;
     if (cudaMalloc(&d_n, cap * sizeof(int)) != cudaSuccess) return MCB_ERR_NOMEM;
     if (cudaMalloc(&d_err, sizeof(int)) != cudaSuccess) return MCB_ERR_NOMEM;
     cudaMemset(d_err, 0, sizeof(int));
-    maps_store.assign(12 * 128 + 64, 0);
+    maps_store.assign(4 * kTcPieces * 128 + 64, 0);
     maps = (unsigned char *)(((uintptr_t)maps_store.data() + 63) & ~(uintptr_t)63);
     steps = ns_schedule(l0, 0.02, 1e-7);
     return MCB_OK;
@@ -389,12 +394,13 @@ int NsProj::configure(int operands_, double l0_) {
 }
 
 void NsProj::destroy() {
-    void *ps[] = {S, S2, T, Wd, Sd, Gd, dptr, Sp, S2p, Tp, Wp, d_live, d_n, d_err};
+    void *ps[] = {S, S2, T, Wd, Sd, Gd, dptr, Sp, S2p, Tp, Wp, d_live, d_n, d_err, d_alpha};
     for (void *p : ps)
         if (p) cudaFree(p);
     S = S2 = T = nullptr;
     Sp = S2p = Tp = Wp = nullptr;
     d_live = d_n = d_err = nullptr;
+    d_alpha = nullptr;
     Wd = Sd = Gd = nullptr;
     dptr = nullptr;
     if (h) cublasDestroy(h);
@@ -413,11 +419,11 @@ int NsProj::set_live(const std::vector<int> &slots, const std::vector<int> &ns, 
                 return MCB_ERR_CUDA;
         }
         if (map_npad != npad) {
-            __nv_bfloat16 *bufs[4] = {Sp, S2p, Tp, Wp};
+            __nv_bfloat16 *bufs[4] = {Wp, Sp, S2p, Tp};
             const size_t tot = stride * (size_t)cap;
             for (int b = 0; b < 4; ++b)
-                for (int p = 0; p < 3; ++p)
-                    if (int rc = tc_make_map(maps + (3 * b + p) * 128, bufs[b] + p * tot, npad, stride, cap))
+                for (int p = 0; p < kTcPieces; ++p)
+                    if (int rc = tc_make_map(maps + (kTcPieces * b + p) * 128, bufs[b] + p * tot, npad, stride, cap))
                         return rc;
             map_npad = npad;
         }
@@ -455,9 +461,26 @@ cublasStatus_t gemm32(cublasHandle_t h, int np, float alpha, void **A, void **B,
 }
 }  // namespace
 
+namespace {
+// plane scales of the tcgen05 path: S and S0 have |entries| <= ||S||_2 <= 1, so
+// sigma = 2 (leading digits <= 64); T = a I + b S^2 has eigenvalues in [a + b, a]
+// with a <= 1.5 sqrt(3) (the schedule's k^2 <= 3), so sigma = 4 (leading digits
+// <= 83).  With digits that small the exact digit-sum groups of every product
+// stay below 2^24 for K <= 1024.  The planes hold q = x 2^7 / sigma.
+constexpr float kPscaleS = 64.0f, kPscaleT = 32.0f;
+constexpr float kUnitSS = 1.0f / 4096.0f;  // sigma_S^2 2^-14
+constexpr float kUnitST = 1.0f / 2048.0f;  // sigma_S sigma_T 2^-14
+// the planes of one plane set (S0, S, S2 or T), tot elements apart
+TcOut planes_out(__nv_bfloat16 *base, size_t tot, size_t stride, int *err, float pscale, float *f32 = nullptr) {
+    TcOut o{f32, nullptr, {}, stride, err, pscale, nullptr};
+    for (int p = 0; p < kTcPieces; ++p) o.p[p] = base + p * tot;
+    return o;
+}
+}  // namespace
+
 int NsProj::tune(cudaStream_t st) {
     const size_t tot = stride * (size_t)cap;
-    TcOut ot{nullptr, nullptr, {Tp, Tp + tot, Tp + 2 * tot}, stride, d_err};
+    TcOut ot = planes_out(Tp, tot, stride, d_err, kPscaleT);
     Tuned t{0, {0.0f, 0.0f}};
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
@@ -467,7 +490,7 @@ int NsProj::tune(cudaStream_t st) {
         float best = 1e30f;
         for (int rep = 0; rep < 4 && rc == MCB_OK; ++rep) {  // first launch warms up
             cudaEventRecord(e0, st);
-            rc = tc_gemm(maps, maps, ot, npad, live, d_live, d_n, 1.0f, 0.0f, st, 1, v);
+            rc = tc_gemm(maps, maps, ot, npad, live, d_live, d_n, 1.0f, 0.0f, kUnitSS, st, 1, v);
             cudaEventRecord(e1, st);
             if (cudaEventSynchronize(e1) != cudaSuccess) rc = MCB_ERR_CUDA;
             float ms = 0.0f;
@@ -496,31 +519,29 @@ int NsProj::check_error(cudaStream_t st) {
 
 void NsProj::split_inputs(cudaStream_t st) {
     const size_t tot = stride * (size_t)cap;
-    TcOut os{nullptr, nullptr, {Sp, Sp + tot, Sp + 2 * tot}, stride, nullptr};
-    TcOut ow{nullptr, nullptr, {Wp, Wp + tot, Wp + 2 * tot}, stride, nullptr};
-    tc_split_f32(S, stride, os, npad, live, d_live, st);
-    tc_split_f64(Wd, stride, ow, npad, live, d_live, st);
+    tc_split_f64(Wd, stride, planes_out(Wp, tot, stride, nullptr, kPscaleS), npad, live, d_live, d_alpha, st);
 }
 
 int NsProj::sign(Slot *d_slots, int ns, int gate, cudaStream_t st) {
     if (live == 0) return MCB_OK;
     if (tc()) {
         const size_t tot = stride * (size_t)cap;
-        __nv_bfloat16 *bufs[3] = {Sp, S2p, Tp};
-        int c = 0, nx = 1;
+        __nv_bfloat16 *bufs[4] = {Wp, Sp, S2p, Tp};
+        auto mp = [&](int b) { return maps + kTcPieces * b * 128; };
+        int c = 0, nx = 1;  // start from S0 (never overwritten: G needs it), then S and S2 in turn
         const double g = 2.0 * (double)npad * npad * npad * live;
         for (size_t i = 0; i < steps.size(); ++i) {
             const NsStep &stp = steps[i];
-            // T = b S^2 + a I (pieces), then S' = S T (pieces; FP32 after the last step)
-            TcOut ot{nullptr, nullptr, {Tp, Tp + tot, Tp + 2 * tot}, stride, d_err};
-            if (int rc = tc_gemm(maps + 3 * c * 128, maps + 3 * c * 128, ot, npad, live, d_live, d_n, stp.b, stp.a, st, 1, variant))
+            // T = b S^2 + a I (planes), then S' = S T (planes; FP32 after the last step)
+            TcOut ot = planes_out(Tp, tot, stride, d_err, kPscaleT);
+            if (int rc = tc_gemm(mp(c), mp(c), ot, npad, live, d_live, d_n, stp.b, stp.a, kUnitSS, st, 1, variant))
                 return rc;
-            __nv_bfloat16 *o = bufs[nx];
-            TcOut os{i + 1 == steps.size() ? S : nullptr, nullptr, {o, o + tot, o + 2 * tot}, stride, d_err};
-            if (int rc = tc_gemm(maps + 3 * c * 128, maps + 3 * 2 * 128, os, npad, live, d_live, d_n, 1.0f, 0.0f, st, 1, variant))
+            TcOut os = planes_out(bufs[nx], tot, stride, d_err, kPscaleS, i + 1 == steps.size() ? S : nullptr);
+            if (int rc = tc_gemm(mp(c), mp(3), os, npad, live, d_live, d_n, 1.0f, 0.0f, kUnitST, st, 1, variant))
                 return rc;
             flops_hi += 2.0 * g;  // algorithmic: two n^3 products per step (the mirror halves the MMAs)
-            std::swap(c, nx);
+            c = nx;
+            nx = nx == 1 ? 2 : 1;
         }
         cur = c;
         launch_ns_finish(d_slots, ns, npad, stride, S, nullptr, gate, st);
@@ -556,8 +577,9 @@ int NsProj::sign(Slot *d_slots, int ns, int gate, cudaStream_t st) {
 int NsProj::product(cudaStream_t st) {
     if (live == 0) return MCB_OK;
     if (tc()) {
-        TcOut og{nullptr, Gd, {nullptr, nullptr, nullptr}, stride, d_err};
-        int rc = tc_gemm(maps + 3 * 3 * 128, maps + 3 * cur * 128, og, npad, live, d_live, d_n, 1.0f, 0.0f, st, 1,
+        // G = W S = alpha (S0 S): the planes of S0 and of the final S, alpha per slot
+        TcOut og{nullptr, Gd, {}, stride, d_err, 1.0f, d_alpha};
+        int rc = tc_gemm(maps, maps + kTcPieces * cur * 128, og, npad, live, d_live, d_n, 1.0f, 0.0f, kUnitSS, st, 1,
                          variant);
         flops_hi += 2.0 * (double)npad * npad * npad * live;
         return rc;

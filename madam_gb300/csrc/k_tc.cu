@@ -1,5 +1,5 @@
 // k_tc.cu -- the Newton-Schulz GEMMs on the 5th-generation tensor cores
-// (tcgen05.mma, operands staged by TMA, accumulator in tensor memory).
+// (tcgen05.mma, operands staged by TMA, accumulators in tensor memory).
 //
 // C = alpha * A * B^T + diag * I_n for a batch of npad x npad row-major matrices
 // (one per live slot).  In the projection A and B are symmetric and commute
@@ -8,27 +8,34 @@
 // its mirror, which keeps the iterates exactly symmetric.  (Without it the
 // rounding's antisymmetric part would grow by the step's slope, ~2.6x, every
 // step, since X (aI + b X X^T) is not a polynomial in X once X is not symmetric.)
-// Every FP32 operand X is carried as three BF16 pieces x_hi + x_mid + x_lo
-// (each the BF16 rounding of what the previous pieces leave), which together
-// hold 24 significant bits.  The product keeps the six piece products whose
-// weight is at least 2^-16 of the leading one -- hi.hi, hi.mid, mid.hi, mid.mid,
-// hi.lo, lo.hi -- and accumulates them in FP32 in tensor memory (hi.hi and the
-// five corrections in two accumulators), so C is FP32-accurate.  The epilogue
-// writes C as FP32, as its own three pieces (the next step's operands) and/or
-// widened to FP64.
 //
-// Tiling: one CTA per 128 x 128 tile of C and slot; K in chunks of 64 BF16
-// (one 128-byte swizzle row).  A stage holds the three pieces of the A and B
-// chunks (96 KB).  Two variants, timed by the autotuner: one stage per CTA, so
-// that two CTAs fit on an SM (shared memory and the 512 tensor-memory columns)
-// and one CTA's TMA loads overlap the other's MMAs; or two stages with one CTA
-// per SM.  One thread issues the TMA copies and the MMAs; all four warps drain
-// the accumulators (32 lanes each) with tcgen05.ld, through shared-memory tiles
-// (row-major for the direct half, column-major for the mirror) so that every
-// global store is coalesced and 64 or 128 bits wide.  Every wait on an
-// mbarrier is bounded: on expiry the CTA records an error code, gives the TMA
-// loads it still has in flight their own bounded wait, skips the rest and
-// releases its tensor memory.
+// Operands are the five BF16 digit planes of tc.h: q = x 2^7 / sigma =
+// sum_a d_a 2^-7a with signed 7-bit digits, plane a holding d_a 2^-7a.  A product
+// is the sum of the nineteen plane products of digit sum <= 5, in four FP32
+// accumulators in tensor memory:
+//   acc0 <- d0 . d0'                 (digit sum 0: integers below 2^24, exact)
+//   acc1 <- d0 . d1' + d1 . d0'       (digit sum 1: multiples of 2^-7, exact)
+//   acc2 <- the three of digit sum 2  (multiples of 2^-14, exact)
+//   acc3 <- the thirteen of digit sum 3, 4, 5 (FP32, ~2^-12 of the total)
+// so C = alpha sigma_A sigma_B 2^-14 (acc0 + acc1 + acc2 + acc3), accurate to
+// ~5e-10 of its norm: FP32 rounding touches only acc3, far below the floor of a
+// three-piece BF16 split accumulated in FP32 (~1e-7 per product), which the
+// Newton-Schulz iteration compounded to ~1e-6 in the projection.  The epilogue
+// sums the four accumulators as an unevaluated float pair (no FP64 arithmetic,
+// which is slow on this part) and writes C as FP32, as FP64 (times a per-slot
+// factor) and/or as the next step's five digit planes.
+//
+// Tiling: one CTA per 128 x 128 tile of C and slot; K in chunks of 32 BF16 (one
+// 64-byte swizzle row).  A stage holds the five planes of the A and B chunks
+// (80 KB).  The four accumulators take all 512 tensor-memory columns, so one CTA
+// runs per SM; the autotuner times two variants: two pipeline stages (TMA of the
+// next chunk under the MMAs of this one) or one.  One thread issues the TMA copies
+// and the MMAs; all four warps drain the accumulators (32 lanes each) with
+// tcgen05.ld, through shared-memory tiles (row-major for the direct half,
+// column-major for the mirror, 64 columns at a time) so that every global store
+// is coalesced.  Every wait on an mbarrier is bounded: on expiry the CTA records
+// an error code, gives the TMA loads it still has in flight their own bounded
+// wait, skips the rest and releases its tensor memory.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -44,24 +51,38 @@
 namespace mcb {
 namespace {
 
-constexpr int BM = 128, BN = 128, BK = 64;
-constexpr int kPieces = 3;
-constexpr int kTileBytes = BM * BK * 2;                   // one piece of one operand chunk (16 KB)
-constexpr int kStageBytes = 2 * kPieces * kTileBytes;    // A and B, three pieces each (96 KB)
-// two variants, picked per matrix order by the autotuner (tc_variant): one stage
-// per CTA with two CTAs per SM, or two stages (TMA of chunk k+1 under the MMAs of
-// chunk k) with one CTA per SM
-constexpr int smem_bytes(int stages) { return stages * kStageBytes + 1024 + 128; }
-constexpr uint32_t kTmemCols = 256;  // two 128-column FP32 accumulators: hi.hi, and the corrections
+constexpr int BM = 128, BN = 128, BK = 32;
+constexpr int kPieces = kTcPieces;
+constexpr int kTileBytes = BM * BK * 2;                // one plane of one operand chunk (8 KB)
+constexpr int kStageBytes = 2 * kPieces * kTileBytes;  // A and B, five planes each (80 KB)
+constexpr int kHalf = BN / 2;                          // epilogue: 64 columns at a time
+constexpr int LDR = kHalf + 2;                         // row-major staging, in float2 (h, l)
+constexpr int LDC = BM + 2;                            // column-major staging, in float2
+constexpr int kEpiBytes = (BM * LDR > kHalf * LDC ? BM * LDR : kHalf * LDC) * 8;
+__host__ __device__ constexpr int cmax(int a, int b) { return a > b ? a : b; }
+// variant 0: two stages; variant 1: one stage.  The four accumulators hold all 512
+// tensor-memory columns, so the shared memory asked for is at least kOneCtaBytes,
+// more than half an SM's: a second CTA never lands on the SM to wait for them.
+constexpr int kStages0 = 2, kStages1 = 1;
+constexpr int kOneCtaBytes = 120 * 1024;
+constexpr int smem_bytes(int stages) {
+    return cmax(cmax(stages * kStageBytes, kEpiBytes) + 1024 + 128, kOneCtaBytes);
+}
+constexpr int kAccs = 4;
+constexpr uint32_t kTmemCols = kAccs * BN;   // 512: acc0 .. acc3
 constexpr long long kSpinLimit = 1ll << 26;  // bounded waits (~a second)
 // the expiry test: no TMA loads are issued (nothing is ever in flight), so the
 // first wait on a full stage runs out after this many polls (~a millisecond)
 constexpr long long kTestSpinLimit = 1ll << 16;
 std::atomic<int> g_test_expiry{0};
 
-// the six piece products (A piece, B piece)
-__constant__ int kProdA[6] = {0, 0, 1, 1, 0, 2};
-__constant__ int kProdB[6] = {0, 1, 0, 1, 2, 0};
+// the nineteen plane products (A plane, B plane, accumulator) of digit sum <= 5;
+// kFirst: the product that starts each accumulator
+constexpr int kProducts = 19;
+__constant__ int kProdA[kProducts] = {0, 0, 1, 0, 1, 2, 0, 1, 2, 3, 0, 1, 2, 3, 4, 1, 2, 3, 4};
+__constant__ int kProdB[kProducts] = {0, 1, 0, 2, 1, 0, 3, 2, 1, 0, 4, 3, 2, 1, 0, 4, 3, 2, 1};
+__constant__ int kProdAcc[kProducts] = {0, 1, 1, 2, 2, 2, 3, 3, 3, 3, 3, 3, 3, 3, 3, 3, 3, 3, 3};
+__constant__ int kFirst[kAccs] = {0, 1, 3, 6};
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -92,14 +113,15 @@ __device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, i
         : "memory");
 }
 
-// shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups 1024 B apart
+// shared-memory matrix descriptor: K-major, 64-byte swizzle (rows of 64 bytes,
+// the pattern repeats every 8 rows = 512 bytes), 8-row groups 512 B apart
 __device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
     uint64_t d = 0;
-    d |= (uint64_t)((addr & 0x3FFFF) >> 4);   // start address
-    d |= (uint64_t)1 << 16;                   // leading byte offset (unused with this swizzle)
-    d |= (uint64_t)(1024 >> 4) << 32;         // stride byte offset
-    d |= (uint64_t)1 << 46;                   // descriptor version
-    d |= (uint64_t)2 << 61;                   // 128-byte swizzle
+    d |= (uint64_t)((addr & 0x3FFFF) >> 4);  // start address
+    d |= (uint64_t)1 << 16;                  // leading byte offset (unused with this swizzle)
+    d |= (uint64_t)(512 >> 4) << 32;         // stride byte offset
+    d |= (uint64_t)1 << 46;                  // descriptor version
+    d |= (uint64_t)4 << 61;                  // 64-byte swizzle
     return d;
 }
 
@@ -118,57 +140,74 @@ __device__ __forceinline__ void mma_commit(uint64_t *bar) {
                  : "memory");
 }
 
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float *v) {
-    uint32_t r[32];
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
+    uint32_t r[16];
     asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
-        "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15}, [%16];"
         : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
-          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
-          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
         : "r"(taddr));
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-    for (int j = 0; j < 32; ++j) v[j] = __uint_as_float(r[j]);
+    for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
 }
 
-__device__ __forceinline__ void split3(float x, __nv_bfloat16 &h, __nv_bfloat16 &m, __nv_bfloat16 &l) {
-    h = __float2bfloat16_rn(x);
-    float r = x - __bfloat162float(h);
-    m = __float2bfloat16_rn(r);
-    l = __float2bfloat16_rn(r - __bfloat162float(m));
+// s + e = a + b exactly (Knuth's two-sum)
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+    s = a + b;
+    const float bp = s - a;
+    e = (a - (s - bp)) + (b - bp);
 }
 
-// three BF16 pieces of four values, packed for 64-bit stores
-__device__ __forceinline__ void split3x4(float4 x, uint2 &h, uint2 &m, uint2 &l) {
-    const float xs[4] = {x.x, x.y, x.z, x.w};
-    __nv_bfloat162 hp[2], mp[2], lp[2];
+// the five digit planes of q = qh + ql (an unevaluated pair): d_a = rint of the
+// remainder times 2^7a, stored as d_a 2^-7a; each subtraction of a digit is exact
+__device__ __forceinline__ void planes(float qh, float ql, __nv_bfloat16 *o) {
+    float rh, rl;
+    two_sum(qh, ql, rh, rl);
+    float w = 1.0f;
 #pragma unroll
-    for (int k = 0; k < 2; ++k) {
-        const float a = xs[2 * k], b = xs[2 * k + 1];
-        hp[k] = __floats2bfloat162_rn(a, b);
-        const float ra = a - __low2float(hp[k]), rb = b - __high2float(hp[k]);
-        mp[k] = __floats2bfloat162_rn(ra, rb);
-        lp[k] = __floats2bfloat162_rn(ra - __low2float(mp[k]), rb - __high2float(mp[k]));
+    for (int a = 0; a < kPieces; ++a) {
+        const float d = rintf(rh);
+        o[a] = __float2bfloat16_rn(d * w);  // a 7-bit integer times a power of two: exact
+        two_sum(rh - d, rl, rh, rl);
+        rh *= 128.0f;
+        rl *= 128.0f;
+        w *= 1.0f / 128.0f;
     }
-    h = make_uint2(*reinterpret_cast<uint32_t *>(&hp[0]), *reinterpret_cast<uint32_t *>(&hp[1]));
-    m = make_uint2(*reinterpret_cast<uint32_t *>(&mp[0]), *reinterpret_cast<uint32_t *>(&mp[1]));
-    l = make_uint2(*reinterpret_cast<uint32_t *>(&lp[0]), *reinterpret_cast<uint32_t *>(&lp[1]));
+}
+
+// coef (acc0 + acc1 + acc2 + acc3) + d as an unevaluated float pair (h, l): the
+// exact accumulators summed by two-sums, the product's rounding error recovered
+// by an FMA, the diagonal added by a two-sum
+__device__ __forceinline__ float2 ff_value(float a0, float a1, float a2, float a3, float coef, float d) {
+    float s, e, e2;
+    two_sum(a0, a1, s, e);
+    two_sum(s, a2, s, e2);
+    e += e2;
+    two_sum(s, a3, s, e2);
+    e += e2;
+    float h = coef * s;
+    float l = fmaf(coef, e, fmaf(coef, s, -h));
+    if (d != 0.0f) {
+        two_sum(h, d, h, e2);
+        l += e2;
+    }
+    two_sum(h, l, h, l);
+    return make_float2(h, l);
 }
 
 struct Maps {
     CUtensorMap a[kPieces], b[kPieces];
 };
 
-
 template <int kStages>
-__global__ void __launch_bounds__(128, 3 - kStages) k_tc_gemm(const __grid_constant__ Maps maps, TcOut out, int npad,
-                                                   const int *live, const int *nlist, float alpha, float diag,
-                                                   int sym, long long spin_limit, int issue_loads) {
+__global__ void __launch_bounds__(128, 1)
+    k_tc_gemm(const __grid_constant__ Maps maps, TcOut out, int npad, const int *live, const int *nlist, float alpha,
+              float diag, float in_scale, int sym, long long spin_limit, int issue_loads) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    uint64_t *full = (uint64_t *)(smem + kStages * kStageBytes);
+    uint64_t *full = (uint64_t *)(smem + cmax(kStages * kStageBytes, kEpiBytes));
     uint64_t *empty = full + kStages;
     uint64_t *done = empty + kStages;
     uint32_t *tmem_slot = (uint32_t *)(done + 1);
@@ -232,14 +271,13 @@ __global__ void __launch_bounds__(128, 3 - kStages) k_tc_gemm(const __grid_const
 #pragma unroll
             for (int kk = 0; kk < BK / 16; ++kk)
 #pragma unroll
-                for (int q = 0; q < 6; ++q) {
-                    // hi.hi into the first accumulator, the five correction products
-                    // (2^-8 of it or less) into the second, so that their bits are
-                    // not lost against the leading term; the epilogue adds the two
-                    uint64_t ad = smem_desc(base + kProdA[q] * kTileBytes + kk * 32);
-                    uint64_t bd = smem_desc(base + (kPieces + kProdB[q]) * kTileBytes + kk * 32);
-                    const uint32_t acc = q == 0 ? (kc | kk) != 0 : !(kc == 0 && kk == 0 && q == 1);
-                    mma_bf16(tmem + (q == 0 ? 0u : (uint32_t)BN), ad, bd, idesc, acc);
+                for (int q = 0; q < kProducts; ++q) {
+                    // each accumulator starts with its first product of the first chunk
+                    const int ac = kProdAcc[q];
+                    const uint64_t ad = smem_desc(base + kProdA[q] * kTileBytes + kk * 32);
+                    const uint64_t bd = smem_desc(base + (kPieces + kProdB[q]) * kTileBytes + kk * 32);
+                    const uint32_t acc = !(kc == 0 && kk == 0 && q == kFirst[ac]);
+                    mma_bf16(tmem + (uint32_t)(ac * BN), ad, bd, idesc, acc);
                 }
             mma_commit(&empty[s]);
             // refill this stage once its MMAs have read it
@@ -253,12 +291,13 @@ __global__ void __launch_bounds__(128, 3 - kStages) k_tc_gemm(const __grid_const
             s_fail = 1;
             // loads still in flight write this CTA's shared memory: give them their
             // own bounded wait before the block can exit and the memory is reused
-            for (int j = landed; j < issued; ++j) mbar_wait(&full[j % kStages], (uint32_t)(j / kStages) & 1u, kSpinLimit);
+            for (int j = landed; j < issued; ++j)
+                mbar_wait(&full[j % kStages], (uint32_t)(j / kStages) & 1u, kSpinLimit);
         }
         mma_commit(done);
     }
     __syncwarp();
-    // every thread waits for the accumulator; the outcome is made block-uniform
+    // every thread waits for the accumulators; the outcome is made block-uniform
     bool ok = mbar_wait(done, 0, kSpinLimit);
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const int bad = __syncthreads_or(!ok || s_fail);
@@ -266,96 +305,107 @@ __global__ void __launch_bounds__(128, 3 - kStages) k_tc_gemm(const __grid_const
         if (tid == 0 && out.err) atomicExch(out.err, MCB_ERR_ITER);
     } else {
         const int n = nlist[blockIdx.y];
-        // Stores go through a shared-memory tile (the stage buffers are free once
-        // the MMAs are done) so that every global store is coalesced and 64 or
-        // 128 bits wide.  Symmetric products: the lower triangle is stored twice,
-        // as (row, col) from a row-major tile and mirrored to (col, row) from a
-        // column-major one (the accumulators are read a second time for it), so
-        // the result is exactly symmetric; diagonal tiles store their lower part.
-        constexpr int LD = BN + 4;  // 16-byte rows, conflict-free 128-bit accesses
-        float *F = (float *)smem;
+        const float coef = alpha * in_scale;
+        const double fscale = out.slot_scale ? out.slot_scale[slot] : 1.0;
+        // Stores go through shared-memory tiles (the stage buffers are free once the
+        // MMAs are done), 64 columns of the tile at a time, so that every global
+        // store is coalesced.  Symmetric products: the lower triangle is stored
+        // twice, as (row, col) from a row-major tile and mirrored to (col, row)
+        // from a column-major one (the accumulators are read a second time for it),
+        // so the result is exactly symmetric; diagonal tiles store their lower part.
+        float2 *F = (float2 *)smem;
         const int r = warp * 32 + lane;
         const bool diag_tile = sym && ti == tj;
         const size_t sb = (size_t)slot * out.stride;
-        auto value = [&](float acc, int row, int col) {
-            return alpha * acc + ((row == col && row < n) ? diag : 0.0f);
-        };
-        // store elements valid_from .. valid_to of four consecutive values (all of
-        // them as vectors); unrolled with register selects, no local memory
-        auto store4 = [&](size_t o, float4 x, int valid_from, int valid_to) {
+        auto dval = [&](int row, int col) { return (row == col && row < n) ? diag : 0.0f; };
+        // store elements valid_from .. valid_to of four consecutive values
+        auto store4 = [&](size_t o, const float2 *x, int valid_from, int valid_to) {
+            __nv_bfloat16 pl[4][kPieces];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) planes(x[e].x * out.pscale, x[e].y * out.pscale, pl[e]);
             if (valid_from == 0 && valid_to == 3) {
-                if (out.f32) *reinterpret_cast<float4 *>(out.f32 + o) = x;
+                if (out.f32)
+                    *reinterpret_cast<float4 *>(out.f32 + o) =
+                        make_float4(x[0].x + x[0].y, x[1].x + x[1].y, x[2].x + x[2].y, x[3].x + x[3].y);
                 if (out.f64) {
-                    reinterpret_cast<double2 *>(out.f64 + o)[0] = make_double2(x.x, x.y);
-                    reinterpret_cast<double2 *>(out.f64 + o)[1] = make_double2(x.z, x.w);
+                    reinterpret_cast<double2 *>(out.f64 + o)[0] = make_double2(
+                        fscale * ((double)x[0].x + (double)x[0].y), fscale * ((double)x[1].x + (double)x[1].y));
+                    reinterpret_cast<double2 *>(out.f64 + o)[1] = make_double2(
+                        fscale * ((double)x[2].x + (double)x[2].y), fscale * ((double)x[3].x + (double)x[3].y));
                 }
                 if (out.p[0]) {
-                    uint2 h, m, l;
-                    split3x4(x, h, m, l);
-                    *reinterpret_cast<uint2 *>(out.p[0] + o) = h;
-                    *reinterpret_cast<uint2 *>(out.p[1] + o) = m;
-                    *reinterpret_cast<uint2 *>(out.p[2] + o) = l;
+#pragma unroll
+                    for (int p = 0; p < kPieces; ++p) {
+                        __nv_bfloat162 a = __halves2bfloat162(pl[0][p], pl[1][p]);
+                        __nv_bfloat162 b = __halves2bfloat162(pl[2][p], pl[3][p]);
+                        *reinterpret_cast<uint2 *>(out.p[p] + o) =
+                            make_uint2(*reinterpret_cast<uint32_t *>(&a), *reinterpret_cast<uint32_t *>(&b));
+                    }
                 }
             } else {
 #pragma unroll
                 for (int e = 0; e < 4; ++e) {
                     if (e < valid_from || e > valid_to) continue;
-                    const float xe = e == 0 ? x.x : (e == 1 ? x.y : (e == 2 ? x.z : x.w));
-                    if (out.f32) out.f32[o + e] = xe;
-                    if (out.f64) out.f64[o + e] = (double)xe;
-                    if (out.p[0]) {
-                        __nv_bfloat16 h, m, l;
-                        split3(xe, h, m, l);
-                        out.p[0][o + e] = h;
-                        out.p[1][o + e] = m;
-                        out.p[2][o + e] = l;
-                    }
+                    if (out.f32) out.f32[o + e] = x[e].x + x[e].y;
+                    if (out.f64) out.f64[o + e] = fscale * ((double)x[e].x + (double)x[e].y);
+                    if (out.p[0])
+#pragma unroll
+                        for (int p = 0; p < kPieces; ++p) out.p[p][o + e] = pl[e][p];
                 }
             }
         };
-        // (1) row-major tile F[r][c] = C(m0 + r, n0 + c)
-        for (int c0 = 0; c0 < BN; c0 += 32) {
-            float v[32], w[32];
-            tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
-            tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(BN + c0), w);
+        for (int half = 0; half < 2; ++half) {
+            const int cb = half * kHalf;
+            // (1) row-major tile F[r][c] = C(m0 + r, n0 + cb + c), c < 64
+            for (int c0 = 0; c0 < kHalf; c0 += 16) {
+                float v[kAccs][16];
 #pragma unroll
-            for (int q = 0; q < 8; ++q) {
-                const int c = c0 + 4 * q;
-                float4 x = make_float4(value(v[4 * q] + w[4 * q], m0 + r, n0 + c),
-                                       value(v[4 * q + 1] + w[4 * q + 1], m0 + r, n0 + c + 1),
-                                       value(v[4 * q + 2] + w[4 * q + 2], m0 + r, n0 + c + 2),
-                                       value(v[4 * q + 3] + w[4 * q + 3], m0 + r, n0 + c + 3));
-                *reinterpret_cast<float4 *>(F + r * LD + c) = x;
-            }
-        }
-        __syncthreads();
-        // direct half: warp per row, lane per 4 columns; diagonal tiles keep col <= row
-        for (int rr = warp; rr < BM; rr += 4) {
-            const int c = 4 * lane;
-            if (diag_tile && c > rr) continue;
-            const float4 x = *reinterpret_cast<const float4 *>(F + rr * LD + c);
-            // on a diagonal tile, columns c .. min(c + 3, rr)
-            store4(sb + (size_t)(m0 + rr) * npad + n0 + c, x, 0, diag_tile ? min(3, rr - c) : 3);
-        }
-        if (sym) {
-            __syncthreads();
-            // (2) column-major tile F[c][r] = C(m0 + r, n0 + c), from the accumulators again
-            for (int c0 = 0; c0 < BN; c0 += 32) {
-                float v[32], w[32];
-                tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
-                tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(BN + c0), w);
+                for (int a = 0; a < kAccs; ++a)
+                    tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(a * BN + cb + c0), v[a]);
 #pragma unroll
-                for (int j = 0; j < 32; ++j) F[(c0 + j) * LD + r] = value(v[j] + w[j], m0 + r, n0 + c0 + j);
+                for (int j = 0; j < 16; ++j)
+                    F[r * LDR + c0 + j] =
+                        ff_value(v[0][j], v[1][j], v[2][j], v[3][j], coef, dval(m0 + r, n0 + cb + c0 + j));
             }
             __syncthreads();
-            // mirrored half: output row n0 + cc, lane per 4 rows of the tile; diagonal
-            // tiles keep rows strictly below the diagonal (rr > cc)
-            for (int cc = warp; cc < BN; cc += 4) {
-                const int rr0 = 4 * lane;
-                const int from = diag_tile ? max(0, cc + 1 - rr0) : 0;
-                if (from >= 4) continue;
-                const float4 x = *reinterpret_cast<const float4 *>(F + cc * LD + rr0);
-                store4(sb + (size_t)(n0 + cc) * npad + m0 + rr0, x, from, 3);
+            // direct half: a half-warp per row, four columns per lane; diagonal tiles
+            // keep col <= row
+            for (int rr = warp * 2 + (lane >> 4); rr < BM; rr += 8) {
+                const int c = 4 * (lane & 15);
+                const int col = cb + c;
+                if (diag_tile && col > rr) continue;
+                float2 x[4];
+#pragma unroll
+                for (int e = 0; e < 4; ++e) x[e] = F[rr * LDR + c + e];
+                store4(sb + (size_t)(m0 + rr) * npad + n0 + col, x, 0, diag_tile ? min(3, rr - col) : 3);
+            }
+            __syncthreads();
+            if (sym) {
+                // (2) column-major tile F[c][r] = C(m0 + r, n0 + cb + c), from the accumulators again
+                for (int c0 = 0; c0 < kHalf; c0 += 16) {
+                    float v[kAccs][16];
+#pragma unroll
+                    for (int a = 0; a < kAccs; ++a)
+                        tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(a * BN + cb + c0), v[a]);
+#pragma unroll
+                    for (int j = 0; j < 16; ++j)
+                        F[(c0 + j) * LDC + r] =
+                            ff_value(v[0][j], v[1][j], v[2][j], v[3][j], coef, dval(m0 + r, n0 + cb + c0 + j));
+                }
+                __syncthreads();
+                // mirrored half: output row n0 + cb + cc, a lane per four rows of the
+                // tile; diagonal tiles keep rows strictly below the diagonal (rr > col)
+                for (int cc = warp; cc < kHalf; cc += 4) {
+                    const int rr0 = 4 * lane;
+                    const int col = cb + cc;
+                    const int from = diag_tile ? max(0, col + 1 - rr0) : 0;
+                    if (from >= 4) continue;
+                    float2 x[4];
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) x[e] = F[cc * LDC + rr0 + e];
+                    store4(sb + (size_t)(n0 + col) * npad + m0 + rr0, x, from, 3);
+                }
+                __syncthreads();
             }
         }
     }
@@ -365,22 +415,33 @@ __global__ void __launch_bounds__(128, 3 - kStages) k_tc_gemm(const __grid_const
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols));
 }
 
-// FP32 (or FP64) matrices -> three BF16 pieces, row-major npad x npad per listed slot
+// FP32 (or FP64) matrices -> the five digit planes of q = x pscale (/ slot_div[slot]),
+// row-major npad x npad per listed slot
 template <typename T>
-__global__ void k_tc_split(const T *src, size_t sstride, TcOut out, int npad, const int *live) {
+__global__ void k_tc_split(const T *src, size_t sstride, TcOut out, int npad, const int *live,
+                           const double *slot_div) {
     const int slot = live[blockIdx.y];
     const size_t tot = (size_t)npad * npad;
     const T *s = src + (size_t)slot * sstride;
+    const double inv = slot_div && slot_div[slot] != 0.0 ? 1.0 / slot_div[slot] : 1.0;
     for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < tot; q += (size_t)gridDim.x * blockDim.x) {
         const size_t o = (size_t)slot * out.stride + q;
-        double x = (double)s[q];
-        __nv_bfloat16 h = __double2bfloat16(x);
-        double r = x - (double)__bfloat162float(h);
-        __nv_bfloat16 m = __double2bfloat16(r);
-        double r2 = r - (double)__bfloat162float(m);
-        out.p[0][o] = h;
-        out.p[1][o] = m;
-        out.p[2][o] = __double2bfloat16(r2);
+        __nv_bfloat16 pl[kPieces];
+        if (sizeof(T) == 4 && !slot_div) {
+            planes((float)s[q] * out.pscale, 0.0f, pl);  // a power-of-two scale: exact
+        } else {
+            // FP64 remainders: each digit subtraction and the times-2^7 are exact
+            double x = (double)s[q] * inv * (double)out.pscale, w = 1.0;
+#pragma unroll
+            for (int a = 0; a < kPieces; ++a) {
+                const double d = rint(x);
+                pl[a] = __float2bfloat16_rn((float)(d * w));
+                x = (x - d) * 128.0;
+                w *= 1.0 / 128.0;
+            }
+        }
+#pragma unroll
+        for (int p = 0; p < kPieces; ++p) out.p[p][o] = pl[p];
     }
 }
 
@@ -403,7 +464,8 @@ EncodeTiled encoder() {
 
 }  // namespace
 
-// a 3D tensor map over `slots` row-major npad x npad BF16 matrices spaced `stride` elements apart
+// a 3D tensor map over `slots` row-major npad x npad BF16 matrices spaced `stride`
+// elements apart; boxes of 32 x 128 elements (64-byte rows, 64-byte swizzle)
 int tc_make_map(void *map, const __nv_bfloat16 *base, int npad, size_t stride, int slots) {
     EncodeTiled enc = encoder();
     if (!enc) return MCB_ERR_CUDA;
@@ -413,7 +475,7 @@ int tc_make_map(void *map, const __nv_bfloat16 *base, int npad, size_t stride, i
     cuuint32_t box[3] = {BK, BM, 1};
     cuuint32_t es[3] = {1, 1, 1};
     CUresult r = enc((CUtensorMap *)map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, (void *)base, dims, strides, box, es,
-                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     return r == CUDA_SUCCESS ? MCB_OK : MCB_ERR_CUDA;
 }
@@ -421,9 +483,9 @@ int tc_make_map(void *map, const __nv_bfloat16 *base, int npad, size_t stride, i
 size_t tc_map_bytes() { return sizeof(CUtensorMap); }
 
 int tc_gemm(const void *amaps, const void *bmaps, const TcOut &out, int npad, int nlive, const int *d_live,
-            const int *d_n, float alpha, float diag, cudaStream_t st, int sym, int variant) {
+            const int *d_n, float alpha, float diag, float in_scale, cudaStream_t st, int sym, int variant) {
     if (nlive <= 0) return MCB_OK;
-    if (npad % BM || npad % BK || variant < 0 || variant >= kTcVariants) return MCB_ERR_ARG;
+    if (npad % BM || npad % BK || npad > 1024 || variant < 0 || variant >= kTcVariants) return MCB_ERR_ARG;
     // the shared-memory limit is a per-device function attribute: set it once on
     // every device that launches the kernel
     static std::atomic<unsigned long long> attr_set{0};
@@ -431,10 +493,10 @@ int tc_gemm(const void *amaps, const void *bmaps, const TcOut &out, int npad, in
     if (cudaGetDevice(&dev) != cudaSuccess) return MCB_ERR_CUDA;
     const unsigned long long bit = (dev >= 0 && dev < 64) ? 1ull << dev : 0ull;
     if (!bit || !(attr_set.load() & bit)) {
-        if (cudaFuncSetAttribute(k_tc_gemm<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes(1)) !=
-                cudaSuccess ||
-            cudaFuncSetAttribute(k_tc_gemm<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes(2)) !=
-                cudaSuccess)
+        if (cudaFuncSetAttribute(k_tc_gemm<kStages0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 smem_bytes(kStages0)) != cudaSuccess ||
+            cudaFuncSetAttribute(k_tc_gemm<kStages1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 smem_bytes(kStages1)) != cudaSuccess)
             return MCB_ERR_CUDA;
         attr_set.fetch_or(bit);
     }
@@ -446,9 +508,11 @@ int tc_gemm(const void *amaps, const void *bmaps, const TcOut &out, int npad, in
     const int test = g_test_expiry.load();
     const long long spins = test ? kTestSpinLimit : kSpinLimit;
     if (variant == 0)
-        k_tc_gemm<1><<<grid, 128, smem_bytes(1), st>>>(m, out, npad, d_live, d_n, alpha, diag, sym, spins, !test);
+        k_tc_gemm<kStages0><<<grid, 128, smem_bytes(kStages0), st>>>(m, out, npad, d_live, d_n, alpha, diag, in_scale,
+                                                                     sym, spins, !test);
     else
-        k_tc_gemm<2><<<grid, 128, smem_bytes(2), st>>>(m, out, npad, d_live, d_n, alpha, diag, sym, spins, !test);
+        k_tc_gemm<kStages1><<<grid, 128, smem_bytes(kStages1), st>>>(m, out, npad, d_live, d_n, alpha, diag, in_scale,
+                                                                     sym, spins, !test);
     return cudaGetLastError() == cudaSuccess ? MCB_OK : MCB_ERR_CUDA;
 }
 
@@ -459,16 +523,15 @@ void tc_split_f32(const float *src, size_t sstride, const TcOut &out, int npad, 
     if (nlive <= 0) return;
     int g = (int)(((size_t)npad * npad + 255) / 256);
     g = g > 128 ? 128 : g;
-    k_tc_split<float><<<dim3(g, nlive), 256, 0, st>>>(src, sstride, out, npad, d_live);
+    k_tc_split<float><<<dim3(g, nlive), 256, 0, st>>>(src, sstride, out, npad, d_live, nullptr);
 }
 void tc_split_f64(const double *src, size_t sstride, const TcOut &out, int npad, int nlive, const int *d_live,
-                  cudaStream_t st) {
+                  const double *slot_div, cudaStream_t st) {
     if (nlive <= 0) return;
     int g = (int)(((size_t)npad * npad + 255) / 256);
     g = g > 128 ? 128 : g;
-    k_tc_split<double><<<dim3(g, nlive), 256, 0, st>>>(src, sstride, out, npad, d_live);
+    k_tc_split<double><<<dim3(g, nlive), 256, 0, st>>>(src, sstride, out, npad, d_live, slot_div);
 }
-
 
 }  // namespace mcb
 

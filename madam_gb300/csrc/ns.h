@@ -13,13 +13,15 @@
 // The schedule starts from l0 (eigenvalues below l0 * alpha in magnitude are
 // not resolved; they change X+ by at most l0 * alpha / 2 each) and ends once
 // 1 - l < 1e-7.  By default (MCB_NS_OPERANDS_SPLIT) every product runs on the
-// library's tcgen05 kernel (k_tc.cu) with operands carried as three BF16 pieces,
-// which is FP32-accurate: one pass of BF16 or TF32 operands cannot resolve
-// eigenvalues below its rounding (~1e-3 of alpha).  The cuBLAS modes (NATIVE:
-// one-pass growth steps and FP32-accurate closing steps, l > 0.9; FP32;
-// CUBLAS_SPLIT) are kept as reference points.  G = W S leaves the accumulators
-// as FP64 (a cuBLAS DGEMM in the cuBLAS modes) and the epilogue forms
-// X+ = (W + (G + G^T)/2) / 2 and Q = X+ - W in FP64.
+// library's tcgen05 kernel (k_tc.cu) with operands carried as five BF16 digit
+// planes whose leading digit-sum groups accumulate exactly (tc.h), accurate to
+// ~5e-10 of the product: one pass of BF16 or TF32 operands cannot resolve
+// eigenvalues below its rounding (~1e-3 of alpha).  The planes of S0 = W / alpha
+// are cut from the FP64 W.  The cuBLAS modes (NATIVE: one-pass growth steps and
+// FP32-accurate closing steps, l > 0.9; FP32; CUBLAS_SPLIT) are kept as reference
+// points.  G = W S = alpha S0 S leaves the accumulators as FP64 (a cuBLAS DGEMM in
+// the cuBLAS modes) and the epilogue forms X+ = (W + (G + G^T)/2) / 2 and
+// Q = X+ - W in FP64.
 #pragma once
 #include <cublas_v2.h>
 #include <cuda_bf16.h>
@@ -47,14 +49,17 @@ struct NsProj {
     int form = 0;        // MCB_PROJ_NS_BF16 or MCB_PROJ_NS_TF32
     int operands = 1;    // MCB_NS_OPERANDS_* of the growth steps
     // SPLIT operands run on the library's own tcgen05 kernel (k_tc.cu): every
-    // matrix as three BF16 pieces, npad a multiple of 128, G = W S from pieces
+    // matrix as five BF16 digit planes (tc.h), npad a multiple of 128, G = alpha S0 S
     bool tc() const { return operands == MCB_NS_OPERANDS_SPLIT; }
-    __nv_bfloat16 *Sp = nullptr, *S2p = nullptr, *Tp = nullptr, *Wp = nullptr;  // 3 * cap * stride each
+    // planes (kTcPieces * cap * stride each): S0 = W / alpha, the iterates S and S2
+    // in turn, and T = b S^2 + a I
+    __nv_bfloat16 *Wp = nullptr, *Sp = nullptr, *S2p = nullptr, *Tp = nullptr;
     int *d_live = nullptr, *d_n = nullptr, *d_err = nullptr;
-    unsigned char *maps = nullptr;  // 12 TMA descriptors: S, S2, T, W pieces (64-byte aligned)
+    double *d_alpha = nullptr;      // alpha = ||W||_F per slot
+    unsigned char *maps = nullptr;  // TMA descriptors: the planes of W, S, S2, T (64-byte aligned)
     std::vector<unsigned char> maps_store;
     int map_npad = 0;
-    int cur = 0;                    // which of S / S2 holds the result of sign()
+    int cur = 0;                    // which plane set (1: S, 2: S2) holds the result of sign()
     // autotuner: tcgen05 kernel variant per (npad, live-slot bucket), with the
     // timings (microseconds per launch) that chose it
     struct Tuned {
@@ -105,14 +110,16 @@ struct NsProj {
     size_t slot_offset(int slot) const { return (size_t)slot * stride; }
     // order of the padded matrices for the live slots' largest n
     int pad(int nmax_live) const { return tc() ? (nmax_live + 127) / 128 * 128 : (nmax_live + 15) / 16 * 16; }
-    // three BF16 pieces of the scaled W (S) and of W for the live slots (tcgen05 path)
+    // the planes of S0 = W / alpha for the live slots, from the FP64 W (tcgen05 path)
     void split_inputs(cudaStream_t st);
     // MCB_ERR_ITER when a bounded wait of a tcgen05 kernel expired (flag reset)
     int check_error(cudaStream_t st);
 };
 
 // kernels (k_ns.cu)
-void launch_ns_prep(Slot *d, int ns, int npad, size_t stride, float *S, double *Wd, int gate, cudaStream_t st);
+// alpha = ||W||_F into s.acc and alpha_out[slot]; Wd = W (FP64, padded), S = W / alpha (FP32)
+void launch_ns_prep(Slot *d, int ns, int npad, size_t stride, float *S, double *Wd, double *alpha_out, int gate,
+                    cudaStream_t st);
 void launch_ns_diag(Slot *d, int ns, int npad, size_t stride, float *T, float a, int gate, cudaStream_t st);
 void launch_ns_finish(Slot *d, int ns, int npad, size_t stride, const float *S, double *Sd, int gate,
                       cudaStream_t st);

@@ -122,7 +122,7 @@ int project_ns(OneSlot &S, int n, int proj) {
     if (rc == MCB_OK) {
         const int npad = P.pad(n);
         rc = P.set_live({0}, {n}, npad, 0);
-        if (rc == MCB_OK) launch_ns_prep(S.d, 1, npad, P.stride, P.S, P.Wd, 0, 0);
+        if (rc == MCB_OK) launch_ns_prep(S.d, 1, npad, P.stride, P.S, P.Wd, P.d_alpha, 0, 0);
         if (rc == MCB_OK && P.tc()) P.split_inputs(0);
         if (rc == MCB_OK) rc = P.sign(S.d, 1, 0, 0);
         if (rc == MCB_OK) rc = P.product(0);
@@ -346,7 +346,7 @@ int mcb_split_gemm(int npad, int batch, const float *A, const float *B, float al
         return p;
     };
     float *dA = (float *)mk(tot * 4), *dB = (float *)mk(tot * 4), *dC = (float *)mk(tot * 4);
-    __nv_bfloat16 *pa = (__nv_bfloat16 *)mk(3 * tot * 2), *pb = (__nv_bfloat16 *)mk(3 * tot * 2);
+    __nv_bfloat16 *pa = (__nv_bfloat16 *)mk(kTcPieces * tot * 2), *pb = (__nv_bfloat16 *)mk(kTcPieces * tot * 2);
     int *live = (int *)mk(batch * sizeof(int)), *nl = (int *)mk(batch * sizeof(int)), *err = (int *)mk(sizeof(int));
     void *maps = mk(6 * tc_map_bytes() + 64);
     int rc = e == cudaSuccess ? MCB_OK : MCB_ERR_NOMEM;
@@ -358,18 +358,35 @@ int mcb_split_gemm(int npad, int batch, const float *A, const float *B, float al
         cudaMemcpy(live, l.data(), batch * sizeof(int), cudaMemcpyHostToDevice);
         cudaMemcpy(nl, nv.data(), batch * sizeof(int), cudaMemcpyHostToDevice);
         cudaMemset(err, 0, sizeof(int));
-        TcOut oa{nullptr, nullptr, {pa, pa + tot, pa + 2 * tot}, nn, nullptr};
-        TcOut ob{nullptr, nullptr, {pb, pb + tot, pb + 2 * tot}, nn, nullptr};
+        // each operand's scale sigma: the smallest power of two >= twice its largest
+        // |entry| (the leading digits are then <= 64, and the exact digit-sum groups
+        // of the product stay below 2^24 for K <= 1024)
+        auto pow2_scale = [&](const float *X) {
+            float mx = 0.0f;
+            for (size_t i = 0; i < tot; ++i) mx = fmaxf(mx, fabsf(X[i]));
+            int e = 0;
+            if (mx > 0.0f) frexpf(mx, &e);  // mx = f 2^e with f in [0.5, 1)
+            return mx > 0.0f ? ldexpf(1.0f, e + 1) : 1.0f;
+        };
+        const float sa = pow2_scale(A), sb = pow2_scale(B);
+        TcOut oa{nullptr, nullptr, {}, nn, nullptr, 128.0f / sa, nullptr};
+        TcOut ob{nullptr, nullptr, {}, nn, nullptr, 128.0f / sb, nullptr};
+        for (int p = 0; p < kTcPieces; ++p) {
+            oa.p[p] = pa + p * tot;
+            ob.p[p] = pb + p * tot;
+        }
         tc_split_f32(dA, nn, oa, npad, batch, live, 0);
         tc_split_f32(dB, nn, ob, npad, batch, live, 0);
         // host-side maps (64-byte aligned), passed by value to the kernel
-        alignas(64) unsigned char hm[6][128];
-        for (int p = 0; p < 3 && rc == MCB_OK; ++p) {
+        alignas(64) unsigned char hm[2 * kTcPieces][128];
+        for (int p = 0; p < kTcPieces && rc == MCB_OK; ++p) {
             rc = tc_make_map(hm[p], oa.p[p], npad, nn, batch);
-            if (rc == MCB_OK) rc = tc_make_map(hm[3 + p], ob.p[p], npad, nn, batch);
+            if (rc == MCB_OK) rc = tc_make_map(hm[kTcPieces + p], ob.p[p], npad, nn, batch);
         }
-        TcOut oc{dC, nullptr, {nullptr, nullptr, nullptr}, nn, err};
-        if (rc == MCB_OK) rc = tc_gemm(hm[0], hm[3], oc, npad, batch, live, nl, alpha, diag, 0, sym, variant);
+        TcOut oc{dC, nullptr, {}, nn, err, 1.0f, nullptr};
+        const float unit = sa * sb / 16384.0f;  // sigma_A sigma_B 2^-14
+        if (rc == MCB_OK)
+            rc = tc_gemm(hm[0], hm[kTcPieces], oc, npad, batch, live, nl, alpha, diag, unit, 0, sym, variant);
         if (rc == MCB_OK && cudaDeviceSynchronize() != cudaSuccess) rc = MCB_ERR_CUDA;
         int herr = 0;
         if (rc == MCB_OK) cudaMemcpy(&herr, err, sizeof(int), cudaMemcpyDeviceToHost);
