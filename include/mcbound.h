@@ -196,7 +196,7 @@ int mcb_project_psd(int n, const double *W, int proj, double *Xp, double *Q, dou
  * counterpart in the reference, which projects host arrays.  W, Xp, Q, Z and
  * evals are the caller's DEVICE buffers (n*n, n*n, n*n, n*n, n doubles); the
  * call allocates nothing: its only scratch is a static device array of the
- * library sized for n <= MCB_NOALLOC_MAX_N (about 2.1 MB on every GPU that
+ * library sized for n <= MCB_NOALLOC_MAX_N (about 5.3 MB on every GPU that
  * loads the library, for as long as it stays loaded).  Larger n returns
  * MCB_ERR_ARG.  Runs on `stream` and returns after it completes, with M on the
  * host.  The first call on a device looks up the scratch's device address

@@ -97,7 +97,11 @@ __global__ void __launch_bounds__(512) k_tridiag(Slot *slots, int gate) {
 }
 
 // ---------------------------------------------------------------------------
-// Sturm count: eigenvalues of T strictly below x
+// Sturm counts: eigenvalues of T strictly below x.
+//
+// sturm(): dstebz's pivot recurrence q_i = d_i - x - e_{i-1}^2 / q_{i-1} with
+// pivmin, one FP64 division per step; used for the largest eigenvalue of the
+// safe bound, whose rigorous error term follows dstebz's analysis.
 __device__ __forceinline__ int sturm(const double *d, const double *e2, int n, double x, double pivmin) {
     int cnt = 0;
     double q = d[0] - x;
@@ -111,17 +115,40 @@ __device__ __forceinline__ int sturm(const double *d, const double *e2, int n, d
     return cnt;
 }
 
-// Eigenvalues of T above vl (ascending) into ev[0..M-1]; M into s.M.
-// largest_only: just the largest eigenvalue into s.lmax.
-__global__ void k_bisect(Slot *slots, double vl, int largest_only, int gate) {
-    Slot &s = slots[blockIdx.x];
-    if (!gated(s, gate)) return;
-    const int n = s.n, tid = threadIdx.x;
-    extern __shared__ double sh[];
-    double *d = sh, *e2 = sh + n, *red = sh + 2 * n;
-    __shared__ int c0;
+// sturm3(): the same count from the three-term Sturm sequence p_0 = 1,
+// p_1 = d_0 - x, p_{i+1} = (d_i - x) p_i - e_{i-1}^2 p_{i-1} (the method of Barth,
+// Martin and Wilkinson, 1967): the number of sign changes.  No division, three
+// FP64 operations per step (FP64 division costs about ten on this part).  The pair
+// (p_i, p_{i+1}) is rescaled by an exact power of two when the larger exponent
+// leaves [-400, 400], and an exact zero takes the sign opposite to its
+// predecessor.  Used for the projection's eigenvalues, which only need to be
+// accurate to a few units in the last place of ||T||.
+__device__ __forceinline__ int sturm3(const double *d, const double *e2, int n, double x) {
+    double p0 = 1.0, p1 = d[0] - x;
+    if (p1 == 0.0) p1 = -0x1p-900;
+    int cnt = p1 < 0.0;
+    for (int i = 1; i < n; ++i) {
+        double p2 = fma(d[i] - x, p1, -e2[i - 1] * p0);
+        if (p2 == 0.0) p2 = p1 < 0.0 ? 0x1p-900 : -0x1p-900;
+        cnt += (__double2hiint(p2) ^ __double2hiint(p1)) < 0;
+        p0 = p1;
+        p1 = p2;
+        const int e0 = (__double2hiint(p0) >> 20) & 0x7ff, e1 = (__double2hiint(p1) >> 20) & 0x7ff;
+        const int em = e0 > e1 ? e0 : e1;
+        if (em > 1023 + 400 || em < 1023 - 400) {
+            const double sc = __hiloint2double((2046 - em) << 20, 0);  // 2^(1023 - em)
+            p0 *= sc;
+            p1 *= sc;
+        }
+    }
+    return cnt;
+}
+
+// Gershgorin interval of T, the largest e_i^2, and d / e^2 into shared memory
+__device__ void tri_setup(const Slot &s, double *d, double *e2, double *red, double &gl, double &gu, double &emax) {
+    const int n = s.n;
     double lo_g = 1e308, hi_g = -1e308, em = 0.0;
-    for (int i = tid; i < n; i += blockDim.x) {
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
         d[i] = s.d[i];
         double el = i > 0 ? fabs(s.e[i - 1]) : 0.0, er = i < n - 1 ? fabs(s.e[i]) : 0.0;
         if (i < n - 1) {
@@ -131,50 +158,80 @@ __global__ void k_bisect(Slot *slots, double vl, int largest_only, int gate) {
         lo_g = fmin(lo_g, d[i] - el - er);
         hi_g = fmax(hi_g, d[i] + el + er);
     }
-    double gl = -block_max(-lo_g, red);
-    double gu = block_max(hi_g, red);
-    double emax = block_max(em, red);
+    gl = -block_max(-lo_g, red);
+    gu = block_max(hi_g, red);
+    emax = block_max(em, red);
+}
+
+// Eigenvalues of T above vl (ascending) into ev[0..M-1]; M into s.M.  The CTAs
+// of a slot (blockIdx.x) split the eigenvalue indices in chunks of blockDim.x,
+// so that a batch of nodes spreads over every SM; each thread bisects one
+// eigenvalue to dstebz's tolerance.
+__global__ void __launch_bounds__(64) k_bisect(Slot *slots, double vl, int gate) {
+    Slot &s = slots[blockIdx.y];
+    if (!gated(s, gate)) return;
+    const int n = s.n, tid = threadIdx.x;
+    const int first = blockIdx.x * blockDim.x;
+    if (first >= n) return;
+    extern __shared__ double sh[];
+    double *d = sh, *e2 = sh + n, *red = sh + 2 * n;
+    __shared__ int c0;
+    double gl, gu, emax;
+    tri_setup(s, d, e2, red, gl, gu, emax);
     const double pivmin = 2.2250738585072014e-308 * fmax(1.0, emax);
-    double tnorm = fmax(fabs(gl), fabs(gu));
+    const double tnorm = fmax(fabs(gl), fabs(gu));
     gl -= 2.0 * tnorm * 2.220446049250313e-16 * n + 2.0 * pivmin;
     gu += 2.0 * tnorm * 2.220446049250313e-16 * n + 2.0 * pivmin;
     // dstebz with ABSTOL <= 0 stops at ULP * max(|gl|, |gu|) (plus the pivmin guard)
     const double atol = 2.220446049250313e-16 * tnorm + 4.0 * pivmin;
-    if (largest_only) {
-        if (tid == 0) {
-            double lo = gl, hi = gu;
-            int it = 0;
-            for (; it < 200; ++it) {
-                double mid = 0.5 * (lo + hi);
-                if (mid <= lo || mid >= hi) break;
-                if (sturm(d, e2, n, mid, pivmin) >= n) hi = mid;  // all eigenvalues below mid
-                else lo = mid;
-                if (hi - lo <= 2.0 * 2.220446049250313e-16 * fmax(fabs(lo), fabs(hi)) + atol) break;
-            }
-            s.lmax = 0.5 * (lo + hi);
-            s.acc[ACC_LMAX_HI] = hi;  // upper end of the final bracket
-            if (it >= 200) s.status = -6;
-        }
-        return;
-    }
-    if (tid == 0) c0 = vl <= gl ? 0 : sturm(d, e2, n, vl, pivmin);
+    if (tid == 0) c0 = vl <= gl ? 0 : sturm3(d, e2, n, vl);
     __syncthreads();
-    int M = n - c0;
-    if (tid == 0) s.M = M;
-    for (int j = tid; j < M; j += blockDim.x) {
-        int idx = c0 + j;
-        double lo = fmax(vl, gl), hi = gu;
-        int it = 0;
-        for (; it < 200; ++it) {
-            double mid = 0.5 * (lo + hi);
-            if (mid <= lo || mid >= hi) break;
-            if (sturm(d, e2, n, mid, pivmin) > idx) hi = mid;
-            else lo = mid;
-            if (hi - lo <= 2.0 * 2.220446049250313e-16 * fmax(fabs(lo), fabs(hi)) + atol) break;
-        }
-        if (it >= 200) s.status = -6;
-        s.ev[j] = 0.5 * (lo + hi);
+    const int M = n - c0;
+    if (blockIdx.x == 0 && tid == 0) s.M = M;
+    const int j = first + tid;
+    if (j >= M) return;
+    const int idx = c0 + j;
+    double lo = fmax(vl, gl), hi = gu;
+    int it = 0;
+    for (; it < 200; ++it) {
+        const double mid = 0.5 * (lo + hi);
+        if (mid <= lo || mid >= hi) break;
+        if (sturm3(d, e2, n, mid) > idx) hi = mid;
+        else lo = mid;
+        if (hi - lo <= 2.0 * 2.220446049250313e-16 * fmax(fabs(lo), fabs(hi)) + atol) break;
     }
+    if (it >= 200) s.status = -6;
+    s.ev[j] = 0.5 * (lo + hi);
+}
+
+// The largest eigenvalue of T into s.lmax, and the upper end of its final
+// bisection bracket into acc[ACC_LMAX_HI] (the safe bound, admm.c:731-752).
+__global__ void k_bisect_max(Slot *slots, int gate) {
+    Slot &s = slots[blockIdx.x];
+    if (!gated(s, gate)) return;
+    const int n = s.n;
+    extern __shared__ double sh[];
+    double *d = sh, *e2 = sh + n, *red = sh + 2 * n;
+    double gl, gu, emax;
+    tri_setup(s, d, e2, red, gl, gu, emax);
+    if (threadIdx.x != 0) return;
+    const double pivmin = 2.2250738585072014e-308 * fmax(1.0, emax);
+    const double tnorm = fmax(fabs(gl), fabs(gu));
+    gl -= 2.0 * tnorm * 2.220446049250313e-16 * n + 2.0 * pivmin;
+    gu += 2.0 * tnorm * 2.220446049250313e-16 * n + 2.0 * pivmin;
+    const double atol = 2.220446049250313e-16 * tnorm + 4.0 * pivmin;
+    double lo = gl, hi = gu;
+    int it = 0;
+    for (; it < 200; ++it) {
+        double mid = 0.5 * (lo + hi);
+        if (mid <= lo || mid >= hi) break;
+        if (sturm(d, e2, n, mid, pivmin) >= n) hi = mid;  // all eigenvalues below mid
+        else lo = mid;
+        if (hi - lo <= 2.0 * 2.220446049250313e-16 * fmax(fabs(lo), fabs(hi)) + atol) break;
+    }
+    s.lmax = 0.5 * (lo + hi);
+    s.acc[ACC_LMAX_HI] = hi;  // upper end of the final bracket
+    if (it >= 200) s.status = -6;
 }
 
 // ---------------------------------------------------------------------------
@@ -182,9 +239,20 @@ __global__ void k_bisect(Slot *slots, double vl, int largest_only, int gate) {
 // (T - lambda I) with partial pivoting, three solves from a fixed pseudo-random
 // start, modified Gram-Schmidt against earlier vectors of the same cluster
 // (eigenvalues closer than 1e-3 ||T||_1).  Vectors go to V (n x M).
-// Scratch per warp: 5 n doubles in s.dwork.
-__device__ void tri_lu(const double *d, const double *e, int n, double lam, double tiny, double *dl,
-                       double *dd, double *du, double *du2, double *piv) {
+//
+// One thread per cluster (a cluster's vectors depend on each other in order;
+// different clusters do not), kInvThreads threads per slot spread over
+// kInvThreads / 64 CTAs, striding over the clusters.  The thread's work arrays
+// (dl, dd, du, du2, piv, b: 6 n doubles) live in s.dwork interleaved across the
+// slot's threads (element i of array k of thread t at (k n + i) kInvThreads + t),
+// so that a warp's accesses are coalesced.
+struct Strided {
+    double *p;
+    __device__ double &operator[](int i) const { return p[(size_t)i * kInvThreads]; }
+};
+
+__device__ void tri_lu(const double *d, const double *e, int n, double lam, double tiny, Strided dl, Strided dd,
+                       Strided du, Strided du2, Strided piv) {
     for (int i = 0; i < n; ++i) dd[i] = d[i] - lam;
     for (int i = 0; i < n - 1; ++i) {
         dl[i] = e[i];
@@ -216,8 +284,7 @@ __device__ void tri_lu(const double *d, const double *e, int n, double lam, doub
         if (fabs(dd[i]) < tiny) dd[i] = dd[i] < 0 ? -tiny : tiny;
 }
 
-__device__ void tri_solve(int n, const double *dl, const double *dd, const double *du, const double *du2,
-                          const double *piv, double *b) {
+__device__ void tri_solve(int n, Strided dl, Strided dd, Strided du, Strided du2, Strided piv, Strided b) {
     for (int i = 0; i < n - 1; ++i) {
         if (piv[i] == 0.0) {
             b[i + 1] -= dl[i] * b[i];
@@ -232,10 +299,10 @@ __device__ void tri_solve(int n, const double *dl, const double *dd, const doubl
     for (int i = n - 3; i >= 0; --i) b[i] = (b[i] - du[i] * b[i + 1] - du2[i] * b[i + 2]) / dd[i];
 }
 
-__global__ void __launch_bounds__(256) k_invit(Slot *slots, int gate) {
-    Slot &s = slots[blockIdx.x];
+__global__ void __launch_bounds__(64) k_invit(Slot *slots, int gate) {
+    Slot &s = slots[blockIdx.y];
     if (!gated(s, gate)) return;
-    const int n = s.n, M = s.M, lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int n = s.n, M = s.M;
     if (M <= 0) return;
     extern __shared__ double sh[];
     double *d = sh, *e = sh + n, *red = sh + 2 * n;
@@ -248,9 +315,9 @@ __global__ void __launch_bounds__(256) k_invit(Slot *slots, int gate) {
         double el = i > 0 ? fabs(s.e[i - 1]) : 0.0, er = i < n - 1 ? fabs(s.e[i]) : 0.0;
         nrm = fmax(nrm, fabs(s.d[i]) + el + er);
     }
-    double onenrm = block_max(nrm, red);
-    double ortol = 1e-3 * onenrm;
-    double tiny = 2.220446049250313e-16 * fmax(onenrm, 1e-300);
+    const double onenrm = block_max(nrm, red);
+    const double ortol = 1e-3 * onenrm;
+    const double tiny = 2.220446049250313e-16 * fmax(onenrm, 1e-300);
     if (threadIdx.x == 0) {
         int c = 0;
         for (int j = 0; j < M; ++j)
@@ -259,47 +326,40 @@ __global__ void __launch_bounds__(256) k_invit(Slot *slots, int gate) {
         ncl = c;
     }
     __syncthreads();
-    double *scr = s.dwork + (size_t)wid * 6 * n;
-    double *dl = scr, *dd = scr + n, *du = scr + 2 * n, *du2 = scr + 3 * n, *piv = scr + 4 * n, *b = scr + 5 * n;
-    for (int cl = wid; cl < ncl; cl += nw) {
-        int j0 = cstart[cl], j1 = cstart[cl + 1];
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;  // the slot's thread, < kInvThreads
+    double *base = s.dwork + t;
+    const size_t stride = (size_t)n * kInvThreads;
+    Strided dl{base}, dd{base + stride}, du{base + 2 * stride}, du2{base + 3 * stride}, piv{base + 4 * stride},
+        b{base + 5 * stride};
+    for (int cl = t; cl < ncl; cl += kInvThreads) {
+        const int j0 = cstart[cl], j1 = cstart[cl + 1];
         for (int j = j0; j < j1; ++j) {
-            double lam = s.ev[j];
-            if (lane == 0) tri_lu(d, e, n, lam, tiny, dl, dd, du, du2, piv);
-            for (int i = lane; i < n; i += 32) {
+            tri_lu(d, e, n, s.ev[j], tiny, dl, dd, du, du2, piv);
+            for (int i = 0; i < n; ++i) {
                 uint64_t h = mix64(((uint64_t)(j + 1) << 32) ^ (uint64_t)(i + 1));
                 b[i] = 2.0 * ((double)(h >> 11) * 0x1.0p-53) - 1.0;
             }
-            __syncwarp();
             double *vj = s.V + (size_t)j * n;
             for (int it = 0; it < 3; ++it) {
-                if (lane == 0) tri_solve(n, dl, dd, du, du2, piv, b);
-                __syncwarp();
+                tri_solve(n, dl, dd, du, du2, piv, b);
                 double ss = 0.0;
-                for (int i = lane; i < n; i += 32) ss += b[i] * b[i];
-                ss = warp_sum(ss);
+                for (int i = 0; i < n; ++i) ss += b[i] * b[i];
                 double inv = ss > 0 ? 1.0 / sqrt(ss) : 0.0;
-                for (int i = lane; i < n; i += 32) b[i] *= inv;
-                __syncwarp();
+                for (int i = 0; i < n; ++i) b[i] *= inv;
                 for (int jp = j0; jp < j; ++jp) {
                     const double *vp = s.V + (size_t)jp * n;
                     double dot = 0.0;
-                    for (int i = lane; i < n; i += 32) dot += vp[i] * b[i];
-                    dot = warp_sum(dot);
-                    for (int i = lane; i < n; i += 32) b[i] -= dot * vp[i];
-                    __syncwarp();
+                    for (int i = 0; i < n; ++i) dot += vp[i] * b[i];
+                    for (int i = 0; i < n; ++i) b[i] -= dot * vp[i];
                 }
                 if (j > j0) {
                     ss = 0.0;
-                    for (int i = lane; i < n; i += 32) ss += b[i] * b[i];
-                    ss = warp_sum(ss);
+                    for (int i = 0; i < n; ++i) ss += b[i] * b[i];
                     inv = ss > 0 ? 1.0 / sqrt(ss) : 0.0;
-                    for (int i = lane; i < n; i += 32) b[i] *= inv;
-                    __syncwarp();
+                    for (int i = 0; i < n; ++i) b[i] *= inv;
                 }
             }
-            for (int i = lane; i < n; i += 32) vj[i] = b[i];
-            __syncwarp();
+            for (int i = 0; i < n; ++i) vj[i] = b[i];
         }
     }
 }
@@ -488,11 +548,14 @@ void launch_tridiag(Slot *d_slots, int nslots, int nmax, int gate, cudaStream_t 
 void launch_bisect(Slot *d_slots, int nslots, int nmax, double vl, int largest_only, int gate,
                    cudaStream_t st) {
     size_t sm = (2 * (size_t)nmax + 40) * sizeof(double);
-    k_bisect<<<nslots, 256, sm, st>>>(d_slots, vl, largest_only, gate);
+    if (largest_only)
+        k_bisect_max<<<nslots, 256, sm, st>>>(d_slots, gate);
+    else
+        k_bisect<<<dim3((nmax + 63) / 64, nslots), 64, sm, st>>>(d_slots, vl, gate);
 }
 void launch_invit(Slot *d_slots, int nslots, int nmax, int gate, cudaStream_t st) {
     size_t sm = (2 * (size_t)nmax + 40) * sizeof(double) + ((size_t)nmax + 1) * sizeof(int);
-    k_invit<<<nslots, 256, sm, st>>>(d_slots, gate);
+    k_invit<<<dim3(kInvThreads / 64, nslots), 64, sm, st>>>(d_slots, gate);
 }
 void launch_backtrans(Slot *d_slots, int nslots, int nmax, int gate, cudaStream_t st) {
     size_t sm = (2 * (size_t)nmax) * sizeof(double);
@@ -523,6 +586,6 @@ void launch_ns_post0(Slot *d_slots, int nslots, int nmax, const double *G, int n
     k_syrk_post<<<dim3(T, nslots), 256, 0, st>>>(d_slots, 3, nullptr, T, G, npad, stride);
 }
 
-size_t eig_dwork_doubles(int nmax) { return (size_t)8 * 6 * nmax; }
+size_t eig_dwork_doubles(int nmax) { return eig_dwork_doubles_max(nmax); }
 
 }  // namespace mcb

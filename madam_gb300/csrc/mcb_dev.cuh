@@ -136,8 +136,10 @@ __host__ __device__ __forceinline__ double cut_scale(int k) {
     return k == 3 ? 1.0 : (k == 5 ? 0.5 : 1.0 / 3.0);
 }
 
-// inverse-iteration workspace of k_invit: 8 warps x 6 n doubles
-constexpr size_t eig_dwork_doubles_max(int n) { return (size_t)48 * (size_t)n; }
+// inverse iteration (k_invit): threads per slot, one per cluster of eigenvalues
+// at a time, and their workspace of 6 n doubles each
+constexpr int kInvThreads = 128;
+constexpr size_t eig_dwork_doubles_max(int n) { return (size_t)6 * kInvThreads * (size_t)n; }
 
 // a slot takes part in a launch: active, and (when gated) its ADMM has not stopped
 __device__ __forceinline__ bool gated(const Slot &s, int gate) { return s.active && !(gate && s.stop); }

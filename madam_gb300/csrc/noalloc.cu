@@ -13,7 +13,7 @@
 // n <= kNoAllocMaxN.
 //
 // The array lives as long as the library is loaded, once per GPU that loads it
-// (about 2.1 MB).  Every call shares it and it keeps the last call's contents;
+// (about 5.3 MB).  Every call shares it and it keeps the last call's contents;
 // everything a call reads from it is written first by the same call, so
 // nothing needs clearing between calls.  Calls whose work overlaps on the GPU
 // (different streams, or different host threads on one device) race on it and
@@ -30,7 +30,7 @@ namespace {
 
 constexpr int kNoAllocMaxN = MCB_NOALLOC_MAX_N;
 constexpr size_t kScratchDoubles = (size_t)kNoAllocMaxN * kNoAllocMaxN   // tridiagonal reduction (A)
-                                   + mcb::eig_dwork_doubles_max(kNoAllocMaxN)  // inverse iteration (6 n per warp)
+                                   + mcb::eig_dwork_doubles_max(kNoAllocMaxN)  // inverse iteration (6 n per thread)
                                    + 3 * (size_t)kNoAllocMaxN                  // d, e, tau
                                    + mcb::kAcc;                                // per-slot accumulators
 
