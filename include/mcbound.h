@@ -152,6 +152,25 @@ int mcb_evaluate(mcb_ctx *ctx, mcb_bab_node *node, int rank, double *bound, mcb_
 int mcb_bound_batch(mcb_ctx *ctx, mcb_bab_node *const *nodes, int count, int rank, double *bounds,
                     mcb_node_stats *stats);
 
+/* ---- several independent problems in one context ---------------------------
+ * No counterpart in the reference, which holds one problem per process (SP,
+ * process_input.c:182-312).  A context holds problem 0 (mcb_create's SL) and any
+ * number added by mcb_add_problem, of order N <= the context's (the slots are
+ * sized for it); each problem keeps its own incumbent, diff, Pent/Hepta_Trials
+ * and triangle budget (10 N under adjust_TriIneq).  mcb_bound_batch_multi bounds
+ * nodes of several problems in one batched pass: node i belongs to problem
+ * problems[i] (its xfixed / sol over that problem's N - 1 variables), and is
+ * bounded exactly as it would be alone in a context of that problem.  A call with
+ * more nodes than the context's batch_max bounds them in chunks of batch_max
+ * nodes of similar subproblem order.  The other calls of this header act on
+ * problem 0. */
+int mcb_add_problem(mcb_ctx *ctx, int N, const double *SL); /* returns the id (>= 1) or MCB_ERR_* */
+int mcb_problem_count(const mcb_ctx *ctx);
+int mcb_bound_batch_multi(mcb_ctx *ctx, mcb_bab_node *const *nodes, const int *problems, int count, int rank,
+                          double *bounds, mcb_node_stats *stats);
+int mcb_set_problem_lb(mcb_ctx *ctx, int problem, double lb, const int *sol);
+double mcb_get_problem_lb(const mcb_ctx *ctx, int problem, int *sol);
+
 /* Serial-equivalent branch-and-bound driver (the MPI master/worker loop of
  * main.c / bab_functions.c:226-334 as one process): root with rank 0 branched
  * at once, then nodes popped in bound order `batch` at a time.  Returns status;

@@ -83,7 +83,22 @@ struct WarmIn {
     int ic = -1;
 };
 
+// One problem of the context (MADAM's SP and the globals SDPbound reads and writes
+// for it): SP->L, the incumbent (Bab_LBGet / Bab_LBUpd, heap.c:15,185), diff
+// (bounding.c:241-243) and the k-gonal trial counts (bounding.c:184-187).
+struct Problem {
+    int N = 0, pb = 0;
+    std::vector<double> SL;  // host copy, N x N column-major
+    double *d_SL = nullptr;  // device copy
+    double LB = 0.0;
+    std::vector<int> best_sol;
+    double diff = 0.0;
+    int pent_trials = 0, hepta_trials = 0;
+    int tri_ineq = 0;  // TriIneq (10 N under adjust_TriIneq, process_input.c:122-123)
+};
+
 struct NodeRun : CutLists {
+    Problem *P = nullptr;  // the node's problem
     mcb_bab_node *node = nullptr;
     int n = 0;
     double fixedvalue = 0, f = 0, basic_bound = 0, bound = 0, oldf = 0, sigma = 0, tol = 0;
@@ -107,14 +122,11 @@ struct NodeRun : CutLists {
 
 struct mcb_ctx {
     mcb_params prm;
-    int N = 0, pb = 0, batch_max = 0, flags = 0;
-    std::vector<double> SL;
-    double *d_SL = nullptr;
+    int N = 0, batch_max = 0, flags = 0;  // N: the order the slots hold (problem 0's)
+    // the problems: 0 from mcb_create, more from mcb_add_problem (order <= N)
+    std::vector<Problem> probs;
     cudaStream_t st = nullptr;
     bool own_stream = false;
-    double LB = 0.0;
-    std::vector<int> best_sol;
-    double diff = 0.0;
     std::mutex lb_mu;
     // slots
     std::vector<Slot> hs;
@@ -510,11 +522,11 @@ int run_chunk(mcb_ctx *c, int ns, int mmax, int emax, int chunk) {
 }
 
 // --- heuristic (heuristic.c), counter streams --------------------------------
-double eval_solution(const mcb_ctx *c, const int *sol) {
+double eval_solution(const Problem &P, const int *sol) {
     double v = 0.0;
-    const int N = c->N, pb = c->pb;
+    const int N = P.N, pb = P.pb;
     for (int i = 0; i < pb; ++i)
-        for (int j = 0; j < pb; ++j) v += c->SL[j + (size_t)i * N] * sol[i] * sol[j];
+        for (int j = 0; j < pb; ++j) v += P.SL[j + (size_t)i * N] * sol[i] * sol[j];
     return v;
 }
 
@@ -552,7 +564,8 @@ void mc_1opt(int *x, const double *L, int N, std::vector<double> &Lx, std::vecto
 
 // GW_heuristic with P0->n hyperplanes (heuristic.c:24-91); result into r.x / r.hval
 void run_heuristic(const mcb_ctx *c, NodeRun &r) {
-    const int N = r.n, M = r.M, num = c->N, pb = c->pb;
+    (void)c;
+    const int N = r.n, M = r.M, num = r.P->N, pb = r.P->pb;
     std::vector<int> tx(N), sol(pb);
     std::vector<double> v(M > 0 ? M : 1), Lx(N), d(N), delta(N);
     std::vector<int> I(N);
@@ -581,7 +594,7 @@ void run_heuristic(const mcb_ctx *c, NodeRun &r) {
             if (r.node->xfixed[i]) sol[i] = r.node->sol[i];
             else sol[i] = (tx[index++] + 1) / 2;
         }
-        double hv = eval_solution(c, sol.data());
+        double hv = eval_solution(*r.P, sol.data());
         if (best < hv) {
             r.x = sol;
             best = hv;
@@ -618,9 +631,9 @@ void run_heuristics(mcb_ctx *c, std::vector<NodeRun *> &all) {
     // updateSolution in slot order (bab_functions.c:114-134)
     for (auto *r : all) {
         r->heur_gpu = false;
-        if (r->hval > c->LB) {
-            c->LB = r->hval;
-            c->best_sol = r->x;
+        if (r->hval > r->P->LB) {
+            r->P->LB = r->hval;
+            r->P->best_sol = r->x;
         }
     }
 }
@@ -651,7 +664,7 @@ int cut_features(mcb_ctx *c, const std::vector<int> &slot_of, const std::vector<
     if (extra) CUDA_TRY(c, h2d(c, c->d_fextra, extra->data(), nc * sizeof(double)));
     {
         Prof p(c, K_LEARN, model ? 2 : 1);
-        launch_cut_features(c->d_slots, c->d_fslot, c->d_fcp, (int)nc, extra ? c->d_fextra : nullptr, c->N, c->d_F,
+        launch_cut_features(c->d_slots, c->d_fslot, c->d_fcp, (int)nc, extra ? c->d_fextra : nullptr, c->d_F,
                             c->st);
         if (model) mlp_forward_device(mlp_impl(model), c->d_F, (int)nc, c->d_pred, c->st);
     }
@@ -674,11 +687,15 @@ void tri_key_to_cp(unsigned int key, int *cp) {
 
 // --- separation --------------------------------------------------------------
 int separate_triangles(mcb_ctx *c, int ns, std::vector<NodeRun *> &runs, std::vector<int> &want) {
-    int K = c->prm.TriIneq;
-    // learned ranking: the 2K most violated candidates, ranked by the scorer
+    // learned ranking: the 2K most violated candidates, ranked by the scorer; K is
+    // the budget of each node's own problem
     const bool learned = (c->flags & MCB_FLAG_LEARNED) && c->scorer;
-    const int Kc = learned ? 2 * K : K;
-    for (int si = 0; si < ns; ++si) c->hs[si].active = want[si];
+    int Kc = 0;
+    for (int si = 0; si < ns; ++si) {
+        c->hs[si].active = want[si];
+        c->hs[si].tri_k = (learned ? 2 : 1) * runs[si]->P->tri_ineq;
+        Kc = std::max(Kc, c->hs[si].tri_k);
+    }
     int rc = upload_slots(c, ns);
     if (rc) return rc;
     {
@@ -693,6 +710,7 @@ int separate_triangles(mcb_ctx *c, int ns, std::vector<NodeRun *> &runs, std::ve
     for (int si = 0; si < ns; ++si) {
         if (!want[si]) continue;
         NodeRun &r = *runs[si];
+        const int K = r.P->tri_ineq;
         double maxv;
         int take_all, need2, n_out, n_bnd;
         tri_sel_readback(c->h_trisel.data(), si, &maxv, &take_all, &need2, &n_out, &n_bnd);
@@ -785,12 +803,12 @@ int separate_kgonal(mcb_ctx *c, int ns, std::vector<NodeRun *> &runs, std::vecto
     int total = 0;
     for (int si = 0; si < ns; ++si) {
         if (want5[si] && runs[si]->n >= 5) {
-            int rr = c->prm.Pent_Trials * 3;
+            int rr = runs[si]->P->pent_trials * 3;
             jobs.push_back({si, 5, rr, total});
             total += rr;
         }
         if (want7[si] && runs[si]->n >= 7) {
-            int rr = c->prm.Hepta_Trials * 4;
+            int rr = runs[si]->P->hepta_trials * 4;
             jobs.push_back({si, 7, rr, total});
             total += rr;
         }
@@ -925,8 +943,9 @@ void purge(NodeRun &r, const std::vector<double> &s) {
 }
 
 void store_fracsol(const mcb_ctx *c, NodeRun &r, const std::vector<double> &lastrow) {
+    (void)c;
     int index = 0;
-    for (int i = 0; i < c->pb; ++i) {
+    for (int i = 0; i < r.P->pb; ++i) {
         if (r.node->xfixed[i]) r.node->fracsol[i] = (double)r.node->sol[i];
         else r.node->fracsol[i] = 0.5 * (lastrow[index++] + 1.0);
     }
@@ -954,7 +973,7 @@ uint64_t node_key(const int *xfixed, const int *sol, int pb) {
 int ns_hyperplanes(mcb_ctx *c, std::vector<NodeRun *> &runs, std::vector<NodeRun *> &hrun) {
     std::vector<int> list;
     std::vector<unsigned long long> keys;
-    int nm = 1;
+    int nm = 1, nh = 1;
     for (size_t q = 0; q < hrun.size(); ++q) {
         NodeRun *r = hrun[q];
         int si = -1;
@@ -964,9 +983,11 @@ int ns_hyperplanes(mcb_ctx *c, std::vector<NodeRun *> &runs, std::vector<NodeRun
         list.push_back(si);
         keys.push_back(key2(r->key, 0x48455552ull + (uint64_t)r->heur_calls));
         nm = std::max(nm, r->n);
+        nh = std::max(nh, r->P->N);
     }
     if (list.empty()) return MCB_OK;
-    const int count = c->N, k = (int)list.size();
+    // as many hyperplanes as the largest listed problem's order; each node keeps its own N
+    const int count = nh, k = (int)list.size();
     const size_t ostride = (size_t)c->N * c->N;
     CUDA_TRY(c, h2d(c, c->d_hlist, list.data(), k * sizeof(int)));
     CUDA_TRY(c, h2d(c, c->d_hkeys, keys.data(), k * sizeof(unsigned long long)));
@@ -982,8 +1003,8 @@ int ns_hyperplanes(mcb_ctx *c, std::vector<NodeRun *> &runs, std::vector<NodeRun
     // the first best hyperplane (heuristic.c's strict comparison) per node
     {
         Prof p(c, K_HEUR, 1);
-        launch_heur_1opt(c->d_slots, c->d_hlist, k, count, c->N, c->d_lists, c->list_stride, c->d_SL, c->d_hsign,
-                         ostride, c->d_hval, c->st);
+        launch_heur_1opt(c->d_slots, c->d_hlist, k, count, c->d_lists, c->list_stride, c->d_hsign, ostride, c->d_hval,
+                         c->st);
     }
     std::vector<double> hv((size_t)k * count);
     CUDA_TRY(c, d2h(c, hv.data(), c->d_hval, hv.size() * sizeof(double)));
@@ -991,13 +1012,13 @@ int ns_hyperplanes(mcb_ctx *c, std::vector<NodeRun *> &runs, std::vector<NodeRun
     for (int q = 0; q < k; ++q) {
         NodeRun &r = *runs[list[q]];
         int bi = 0;
-        for (int h = 1; h < count; ++h)
+        for (int h = 1; h < r.P->N; ++h)
             if (hv[(size_t)q * count + h] > hv[(size_t)q * count + bi]) bi = h;
         best.resize(r.n);
         CUDA_TRY(c, d2h(c, best.data(), c->d_hsign + (size_t)q * ostride + (size_t)bi * r.n, r.n));
-        r.x.assign(c->pb, 0);
+        r.x.assign(r.P->pb, 0);
         int idx = 0;
-        for (int i = 0; i < c->pb; ++i) {
+        for (int i = 0; i < r.P->pb; ++i) {
             if (r.node->xfixed[i]) r.x[i] = r.node->sol[i];
             else r.x[i] = best[idx++] ? 0 : 1;
         }
@@ -1016,9 +1037,9 @@ void apply_warm_start(mcb_ctx *c, NodeRun &r) {
     if (it == c->warm_in.end() || !it->second.rec) return;
     const NodeRecord &P = *it->second.rec;
     if (P.pred.size() != P.size()) return;
-    std::vector<int> loc(c->N, -1);
+    std::vector<int> loc(r.P->N, -1);
     for (size_t v = 0; v < r.U.size(); ++v) loc[r.U[v]] = (int)v;
-    loc[c->N - 1] = r.n - 1;
+    loc[r.P->N - 1] = r.n - 1;
     for (size_t q = 0; q < P.size(); ++q) {
         const int k = P.k[q];
         int v[7];
@@ -1059,7 +1080,7 @@ int make_record(mcb_ctx *c, int si, NodeRun &r, std::shared_ptr<NodeRecord> &out
     NodeRecord &R = *out;
     std::vector<int> so, cps;
     std::vector<double> ex;
-    auto glob = [&](int v) { return v == r.n - 1 ? c->N - 1 : r.U[v]; };
+    auto glob = [&](int v) { return v == r.n - 1 ? r.P->N - 1 : r.U[v]; };
     auto add = [&](int k, int type, const int *v, double dual) {
         R.k.push_back(k);
         R.type.push_back(type);
@@ -1089,7 +1110,8 @@ int make_record(mcb_ctx *c, int si, NodeRun &r, std::shared_ptr<NodeRecord> &out
 }
 
 // --- the batched SDPbound ----------------------------------------------------
-int bound_batch(mcb_ctx *c, mcb_bab_node *const *nodes, int count, int rank, double *bounds, mcb_node_stats *stats) {
+int bound_batch(mcb_ctx *c, mcb_bab_node *const *nodes, const int *probs, int count, int rank, double *bounds,
+                mcb_node_stats *stats) {
     auto t0 = std::chrono::steady_clock::now();
     auto t_last = t0;
     // wall time since the previous tick goes to `phase`
@@ -1098,7 +1120,7 @@ int bound_batch(mcb_ctx *c, mcb_bab_node *const *nodes, int count, int rank, dou
         c->host_s[phase] += std::chrono::duration<double>(t - t_last).count();
         t_last = t;
     };
-    const int N = c->N, pb = c->pb;
+    const int N = c->N;
     const mcb_params &P = c->prm;
     int rc;
     std::vector<NodeRun> R(count);
@@ -1108,6 +1130,8 @@ int bound_batch(mcb_ctx *c, mcb_bab_node *const *nodes, int count, int rank, dou
         NodeRun &r = R[si];
         runs[si] = &r;
         r.node = nodes[si];
+        r.P = &c->probs[probs ? probs[si] : 0];
+        const int pb = r.P->pb;
         int *ls = &lists[(size_t)si * c->list_stride];
         std::vector<int> U, F1, FX, FS;
         for (int i = 0; i < pb; ++i) {
@@ -1130,14 +1154,16 @@ int bound_batch(mcb_ctx *c, mcb_bab_node *const *nodes, int count, int rank, dou
         r.sigma = P.sigma0;
         r.tol = P.tol0;
         Slot &s = c->hs[si];
+        s.SL = r.P->d_SL; s.N = r.P->N;
         s.n = r.n; s.m = 0; s.ne = 0; s.active = 1; s.M = 0; s.sigma = r.sigma; s.tol = r.tol;
         s.nbit = 0; s.stop = 0; s.status = 0;
     }
-    int pend_pent = 0, pend_hept = 0;
+    // the k-gonal trial growth of give-ups (bounding.c:184-187), per problem, applied after the batch
+    std::map<Problem *, std::pair<int, int>> pend;
     const int ns = count;
     CUDA_TRY(c, h2d(c, c->d_lists, lists.data(), lists.size() * sizeof(int)));
     if ((rc = upload_slots(c, ns))) return rc;
-    { Prof p(c, K_SUB, 1); launch_subproblem(c->d_slots, ns, c->d_lists, c->list_stride, c->d_SL, N, c->d_fixed, c->st); }
+    { Prof p(c, K_SUB, 1); launch_subproblem(c->d_slots, ns, c->d_lists, c->list_stride, c->d_fixed, c->st); }
     std::vector<double> fixedv(ns);
     CUDA_TRY(c, d2h(c, fixedv.data(), c->d_fixed, ns * sizeof(double)));
     // IPM (ipm_mc_pk.c), batched until every slot has converged
@@ -1177,8 +1203,8 @@ int bound_batch(mcb_ctx *c, mcb_bab_node *const *nodes, int count, int rank, dou
         NodeRun &r = R[si];
         r.bound = r.f + r.fixedvalue;
         if (r.status) { r.done = 1; continue; }
-        if (r.bound < c->LB + 1.0) { r.prune = 1; r.done = 1; continue; }
-        if (P.use_diff && rank != 0 && r.bound > c->LB + c->diff + 1.0) { r.giveup = 1; r.done = 1; continue; }
+        if (r.bound < r.P->LB + 1.0) { r.prune = 1; r.done = 1; continue; }
+        if (P.use_diff && rank != 0 && r.bound > r.P->LB + r.P->diff + 1.0) { r.giveup = 1; r.done = 1; continue; }
         want[si] = 1;
     }
     if ((c->flags & MCB_FLAG_LEARNED) && c->warm)
@@ -1302,7 +1328,7 @@ int bound_batch(mcb_ctx *c, mcb_bab_node *const *nodes, int count, int rank, dou
             r.tol = r.tol * P.scaleTol;
             if (r.tol < P.minTol) r.tol = P.minTol;
             r.bound = r.f + r.fixedvalue;
-            r.prune = r.bound < c->LB + 1.0;
+            r.prune = r.bound < r.P->LB + 1.0;
             if (!r.prune) {
                 if (c->proj == MCB_PROJ_FP64) {
                     double sg = acc[(size_t)si * kAcc + ACC_SIGMA_LAST];
@@ -1325,14 +1351,17 @@ int bound_batch(mcb_ctx *c, mcb_bab_node *const *nodes, int count, int rank, dou
             if (!live[si]) continue;
             NodeRun &r = R[si];
             if (r.status) continue;
-            if (!r.prune) r.prune = r.bound < c->LB + 1.0;
-            double gap = r.bound - c->LB;
+            if (!r.prune) r.prune = r.bound < r.P->LB + 1.0;
+            double gap = r.bound - r.P->LB;
             if (r.count == P.triag_iter + P.pent_iter + P.hept_iter)
                 if (gap - 1.0 > (r.oldf - r.f) * (P.max_outer_iter - r.count)) r.giveup = 1;
             if (r.count == P.max_outer_iter)
                 if (gap - 1.0 > (r.oldf - r.f) * P.extra_iter) r.giveup = 1;
             if (r.count == P.max_outer_iter + P.extra_iter) r.giveup = 1;
-            if (rank != 0 && r.giveup && !r.prune) { pend_pent += 60; pend_hept += 50; }
+            if (rank != 0 && r.giveup && !r.prune) {
+                pend[r.P].first += 60;
+                pend[r.P].second += 50;
+            }
             if (!r.prune && !r.giveup) want3[si] = 1;
         }
         // purge with the new duals, then separate
@@ -1389,7 +1418,7 @@ int bound_batch(mcb_ctx *c, mcb_bab_node *const *nodes, int count, int rank, dou
     for (int si = 0; si < ns; ++si) {
         NodeRun &r = R[si];
         r.bound = r.f + r.fixedvalue;
-        if (rank == 0 && r.count > 0 && !r.status) c->diff = r.basic_bound - r.bound;  // bounding.c:241-243
+        if (rank == 0 && r.count > 0 && !r.status) r.P->diff = r.basic_bound - r.bound;  // bounding.c:241-243
         if (bounds) bounds[si] = r.bound;
         if (r.status && ret == MCB_OK) ret = r.status;
         if (stats) {
@@ -1408,10 +1437,31 @@ int bound_batch(mcb_ctx *c, mcb_bab_node *const *nodes, int count, int rank, dou
             S.seconds = secs;
         }
     }
-    c->prm.Pent_Trials += pend_pent;
-    c->prm.Hepta_Trials += pend_hept;
+    for (auto &kv : pend) {
+        kv.first->pent_trials += kv.second.first;
+        kv.first->hepta_trials += kv.second.second;
+    }
     if (ret != MCB_OK && c->err.empty()) c->err = "a device iteration cap or factorisation failed";
     return ret;
+}
+
+// a new problem of the context (its SP->L on the host and the device); its id or -1
+int add_problem(mcb_ctx *c, int N, const double *SL) {
+    Problem P;
+    P.N = N;
+    P.pb = N - 1;
+    P.SL.assign(SL, SL + (size_t)N * N);
+    P.best_sol.assign(P.pb, 0);
+    P.pent_trials = c->prm.Pent_Trials;
+    P.hepta_trials = c->prm.Hepta_Trials;
+    P.tri_ineq = c->prm.adjust_TriIneq ? 10 * N : c->prm.TriIneq;
+    if (cudaMalloc(&P.d_SL, (size_t)N * N * sizeof(double)) != cudaSuccess) return -1;
+    if (cudaMemcpy(P.d_SL, SL, (size_t)N * N * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess) {
+        cudaFree(P.d_SL);
+        return -1;
+    }
+    c->probs.push_back(std::move(P));
+    return (int)c->probs.size() - 1;
 }
 
 }  // namespace
@@ -1453,17 +1503,12 @@ mcb_ctx *mcb_create(const mcb_params *params, int N, const double *SL, int batch
     c->prm = *params;
     if (c->prm.adjust_TriIneq) c->prm.TriIneq = N * 10;  // process_input.c:122-123
     c->N = N;
-    c->pb = N - 1;
     c->batch_max = batch_max;
     c->flags = flags;
-    c->SL.assign(SL, SL + (size_t)N * N);
-    c->best_sol.assign(c->pb, 0);
     if (stream) c->st = (cudaStream_t)stream;
     else { cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking); c->own_stream = true; }
-    int rc = MCB_OK;
+    int rc = add_problem(c, N, SL) == 0 ? MCB_OK : MCB_ERR_CUDA;
     auto chk = [&](cudaError_t e) { if (e != cudaSuccess && rc == MCB_OK) { rc = MCB_ERR_CUDA; c->err = cudaGetErrorString(e); } };
-    chk(cudaMalloc(&c->d_SL, (size_t)N * N * sizeof(double)));
-    if (rc == MCB_OK) chk(cudaMemcpy(c->d_SL, SL, (size_t)N * N * sizeof(double), cudaMemcpyHostToDevice));
     c->hs.assign(batch_max, Slot());
     c->mem.assign(batch_max, SlotMem());
     for (int i = 0; i < batch_max && rc == MCB_OK; ++i) rc = alloc_slot(c, i);
@@ -1505,7 +1550,9 @@ void mcb_destroy(mcb_ctx *c) {
     for (auto &m : c->mem) free_slot(m);
     if (c->gexec) cudaGraphExecDestroy(c->gexec);
     c->ns.destroy();
-    void *ps[] = {c->d_SL, c->d_slots, c->d_partials, c->d_lists, c->d_fixed, c->d_trisel, c->d_tout, c->d_toutv,
+    for (auto &P : c->probs)
+        if (P.d_SL) cudaFree(P.d_SL);
+    void *ps[] = {c->d_slots, c->d_partials, c->d_lists, c->d_fixed, c->d_trisel, c->d_tout, c->d_toutv,
                   c->d_tbnd, c->d_tbndv, c->d_sajobs, c->d_perm, c->d_saout, c->d_saval,
                   c->d_hlist, c->d_hkeys, c->d_hsign, c->d_hval, c->d_fslot, c->d_fcp, c->d_fextra, c->d_F, c->d_pred};
     for (void *p : ps)
@@ -1516,20 +1563,31 @@ void mcb_destroy(mcb_ctx *c) {
     delete c;
 }
 
-void mcb_set_lb(mcb_ctx *c, double lb, const int *sol) {
-    if (!c) return;
-    c->LB = lb;
-    if (sol) c->best_sol.assign(sol, sol + c->pb);
+void mcb_set_lb(mcb_ctx *c, double lb, const int *sol) { mcb_set_problem_lb(c, 0, lb, sol); }
+double mcb_get_lb(const mcb_ctx *c, int *sol) { return mcb_get_problem_lb(c, 0, sol); }
+int mcb_set_problem_lb(mcb_ctx *c, int problem, double lb, const int *sol) {
+    if (!c || problem < 0 || problem >= (int)c->probs.size()) return MCB_ERR_ARG;
+    Problem &P = c->probs[problem];
+    P.LB = lb;
+    if (sol) P.best_sol.assign(sol, sol + P.pb);
+    return MCB_OK;
 }
-double mcb_get_lb(const mcb_ctx *c, int *sol) {
-    if (!c) return 0.0;
-    if (sol) memcpy(sol, c->best_sol.data(), c->pb * sizeof(int));
-    return c->LB;
+double mcb_get_problem_lb(const mcb_ctx *c, int problem, int *sol) {
+    if (!c || problem < 0 || problem >= (int)c->probs.size()) return 0.0;
+    const Problem &P = c->probs[problem];
+    if (sol) memcpy(sol, P.best_sol.data(), P.pb * sizeof(int));
+    return P.LB;
 }
 void mcb_set_diff(mcb_ctx *c, double d) {
-    if (c) c->diff = d;
+    if (c) c->probs[0].diff = d;
 }
-double mcb_get_diff(const mcb_ctx *c) { return c ? c->diff : 0.0; }
+double mcb_get_diff(const mcb_ctx *c) { return c ? c->probs[0].diff : 0.0; }
+int mcb_add_problem(mcb_ctx *c, int N, const double *SL) {
+    if (!c || !SL || N < 2 || N > c->N) return MCB_ERR_ARG;
+    const int id = add_problem(c, N, SL);
+    return id < 0 ? MCB_ERR_CUDA : id;
+}
+int mcb_problem_count(const mcb_ctx *c) { return c ? (int)c->probs.size() : 0; }
 int mcb_set_models(mcb_ctx *c, mcb_mlp *scorer, mcb_mlp *warm) {
     if (!c) return MCB_ERR_ARG;
     if ((scorer && mcb_mlp_num_params(scorer) <= 0) || (warm && mcb_mlp_num_params(warm) <= 0)) return MCB_ERR_ARG;
@@ -1626,25 +1684,61 @@ int mcb_ns_schedule(const mcb_ctx *c, int cap, float *a, float *b, int *accurate
 }
 void mcb_set_trials(mcb_ctx *c, int p, int h) {
     if (!c) return;
-    c->prm.Pent_Trials = p;
-    c->prm.Hepta_Trials = h;
+    c->probs[0].pent_trials = p;
+    c->probs[0].hepta_trials = h;
 }
 void mcb_get_trials(const mcb_ctx *c, int *p, int *h) {
-    if (p) *p = c ? c->prm.Pent_Trials : 0;
-    if (h) *h = c ? c->prm.Hepta_Trials : 0;
+    if (p) *p = c ? c->probs[0].pent_trials : 0;
+    if (h) *h = c ? c->probs[0].hepta_trials : 0;
+}
+
+int mcb_bound_batch_multi(mcb_ctx *c, mcb_bab_node *const *nodes, const int *problems, int count, int rank,
+                          double *bounds, mcb_node_stats *stats) {
+    if (!c || !nodes || count < 1) return MCB_ERR_ARG;
+    for (int i = 0; i < count; ++i)
+        if (!nodes[i] || (problems && (problems[i] < 0 || problems[i] >= (int)c->probs.size()))) return MCB_ERR_ARG;
+    c->err.clear();
+    int rc = MCB_OK;
+    if (!problems || count <= c->batch_max) {
+        for (int off = 0; off < count && rc == MCB_OK; off += c->batch_max) {
+            int k = std::min(c->batch_max, count - off);
+            rc = bound_batch(c, nodes + off, problems ? problems + off : nullptr, k, rank,
+                             bounds ? bounds + off : nullptr, stats ? stats + off : nullptr);
+        }
+        return rc;
+    }
+    // more nodes than slots: chunks of nodes with similar subproblem orders (the
+    // tensor-core path pads a chunk to its largest order), in decreasing order
+    std::vector<int> ord(count), nsub(count);
+    for (int i = 0; i < count; ++i) {
+        const Problem &P = c->probs[problems[i]];
+        int fixed = 0;
+        for (int v = 0; v < P.pb; ++v) fixed += nodes[i]->xfixed[v] != 0;
+        nsub[i] = P.pb - fixed + 1;
+        ord[i] = i;
+    }
+    std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return nsub[a] > nsub[b]; });
+    std::vector<mcb_bab_node *> nd(count);
+    std::vector<int> pr(count);
+    for (int i = 0; i < count; ++i) {
+        nd[i] = nodes[ord[i]];
+        pr[i] = problems[ord[i]];
+    }
+    std::vector<double> bo(count);
+    std::vector<mcb_node_stats> so(count);
+    for (int off = 0; off < count && rc == MCB_OK; off += c->batch_max) {
+        int k = std::min(c->batch_max, count - off);
+        rc = bound_batch(c, nd.data() + off, pr.data() + off, k, rank, bo.data() + off, so.data() + off);
+    }
+    for (int i = 0; i < count; ++i) {
+        if (bounds) bounds[ord[i]] = bo[i];
+        if (stats) stats[ord[i]] = so[i];
+    }
+    return rc;
 }
 
 int mcb_bound_batch(mcb_ctx *c, mcb_bab_node *const *nodes, int count, int rank, double *bounds, mcb_node_stats *stats) {
-    if (!c || !nodes || count < 1) return MCB_ERR_ARG;
-    for (int i = 0; i < count; ++i)
-        if (!nodes[i]) return MCB_ERR_ARG;
-    c->err.clear();
-    int rc = MCB_OK;
-    for (int off = 0; off < count && rc == MCB_OK; off += c->batch_max) {
-        int k = std::min(c->batch_max, count - off);
-        rc = bound_batch(c, nodes + off, k, rank, bounds ? bounds + off : nullptr, stats ? stats + off : nullptr);
-    }
-    return rc;
+    return mcb_bound_batch_multi(c, nodes, nullptr, count, rank, bounds, stats);
 }
 
 int mcb_evaluate(mcb_ctx *c, mcb_bab_node *node, int rank, double *bound, mcb_node_stats *st) {
@@ -1729,11 +1823,11 @@ int branching_var(const mcb_ctx *c, const mcb_bab_node *node) {
     int ic = -1;
     if (c->prm.branchingStrategy == 0) {
         double mx = -kBig;
-        for (int i = 0; i < c->pb; ++i)
+        for (int i = 0; i < c->probs[0].pb; ++i)
             if (!node->xfixed[i] && fabs(0.5 - node->fracsol[i]) > mx) { ic = i; mx = fabs(0.5 - node->fracsol[ic]); }
     } else {
         double mn = kBig;
-        for (int i = 0; i < c->pb; ++i)
+        for (int i = 0; i < c->probs[0].pb; ++i)
             if (!node->xfixed[i] && fabs(0.5 - node->fracsol[i]) < mn) { ic = i; mn = fabs(0.5 - node->fracsol[ic]); }
     }
     return ic;
@@ -1757,11 +1851,11 @@ int mcb_bab(mcb_ctx *c, int batch, int max_nodes, double *opt, int *sol, double 
     if (log && lc < log_cap) log[lc++] = st;
     if (root_bound) *root_bound = rb;
     root->upper_bound = rb;
-    if (rc == MCB_OK && c->LB + 1.0 < rb && !c->prm.root) {
+    if (rc == MCB_OK && c->probs[0].LB + 1.0 < rb && !c->prm.root) {
         int ic = branching_var(c, root);
         std::shared_ptr<NodeRecord> rec = c->last_records.empty() ? nullptr : c->last_records[0];
         for (int xic = 0; xic <= 1 && ic >= 0; ++xic) {
-            mcb_bab_node *ch = child_of(root, c->pb, ic, xic);
+            mcb_bab_node *ch = child_of(root, c->probs[0].pb, ic, xic);
             if (rec && rec->size()) c->warm_in[ch] = WarmIn{rec, ic};
             h.push(ch);
             nodes++;
@@ -1794,11 +1888,11 @@ int mcb_bab(mcb_ctx *c, int batch, int max_nodes, double *opt, int *sol, double 
                 if (c->flags & MCB_FLAG_LOG) log_warm_pairs(c, it->second, rec);
                 c->warm_in.erase(it);
             }
-            if (rc == MCB_OK && c->LB + 1.0 < b[a]) {
+            if (rc == MCB_OK && c->probs[0].LB + 1.0 < b[a]) {
                 int ic = branching_var(c, cur[a]);
                 if (ic >= 0) {
                     for (int xic = 0; xic <= 1; ++xic) {
-                        mcb_bab_node *ch = child_of(cur[a], c->pb, ic, xic);
+                        mcb_bab_node *ch = child_of(cur[a], c->probs[0].pb, ic, xic);
                         if (rec && rec->size()) c->warm_in[ch] = WarmIn{rec, ic};
                         h.push(ch);
                     }
@@ -1810,15 +1904,15 @@ int mcb_bab(mcb_ctx *c, int batch, int max_nodes, double *opt, int *sol, double 
     }
     // the open nodes' bounds (their parents' bounds) bound every cut still unexplored
     for (auto *n : h.d) {
-        if (c->LB + 1.0 < n->upper_bound) {
+        if (c->probs[0].LB + 1.0 < n->upper_bound) {
             c->bab_open_bound = std::max(c->bab_open_bound, n->upper_bound);
             c->bab_open_nodes++;
         }
         free(n);
     }
     c->warm_in.clear();
-    if (opt) *opt = c->LB;
-    if (sol) memcpy(sol, c->best_sol.data(), c->pb * sizeof(int));
+    if (opt) *opt = c->probs[0].LB;
+    if (sol) memcpy(sol, c->probs[0].best_sol.data(), c->probs[0].pb * sizeof(int));
     if (nodes_out) *nodes_out = nodes;
     if (log_count) *log_count = lc;
     return rc;

@@ -20,7 +20,7 @@ namespace mcb {
 namespace {
 
 __global__ void __launch_bounds__(128) k_cut_features(const Slot *slots, const int *slot_of, const int *cps, int ncut,
-                                                      const double *extra, int N, float *F) {
+                                                      const double *extra, float *F) {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= ncut) return;
     const Slot &s = slots[slot_of[q]];
@@ -54,17 +54,17 @@ __global__ void __launch_bounds__(128) k_cut_features(const Slot *slots, const i
     f[4] = (float)mx;
     f[5] = (float)(wsum / pairs / (1.0 + wmax));
     f[6] = (float)edges / (float)pairs;
-    f[7] = (float)n / (float)N;
+    f[7] = (float)n / (float)s.N;
     f[8] = extra ? (float)log1p(fmax(extra[q], 0.0)) : 0.0f;
     f[9] = (float)last;
 }
 
 }  // namespace
 
-void launch_cut_features(const Slot *d_slots, const int *slot_of, const int *cps, int ncut, const double *extra, int N,
+void launch_cut_features(const Slot *d_slots, const int *slot_of, const int *cps, int ncut, const double *extra,
                          float *F, cudaStream_t st) {
     if (ncut <= 0) return;
-    k_cut_features<<<(ncut + 127) / 128, 128, 0, st>>>(d_slots, slot_of, cps, ncut, extra, N, F);
+    k_cut_features<<<(ncut + 127) / 128, 128, 0, st>>>(d_slots, slot_of, cps, ncut, extra, F);
 }
 
 }  // namespace mcb

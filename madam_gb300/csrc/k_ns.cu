@@ -160,9 +160,9 @@ __global__ void __launch_bounds__(256) k_heur_sign(Slot *slots, const int *list,
 // here is exact and independent of order.  Lane l owns elements l + 32 j.
 // signs: n bytes per hyperplane (1 = -1), overwritten with the 1-opt result;
 // hval[q * count + h] = the cut value.
-__global__ void __launch_bounds__(128) k_heur_1opt(const Slot *slots, const int *list, int count, int N,
-                                                   const int *lists, int list_stride, const double *SL,
-                                                   unsigned char *signs, size_t sstride, double *hval) {
+__global__ void __launch_bounds__(128) k_heur_1opt(const Slot *slots, const int *list, int count, const int *lists,
+                                                   int list_stride, unsigned char *signs, size_t sstride,
+                                                   double *hval) {
     constexpr int PER = kNmax / 32;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int h = blockIdx.x * 4 + warp;
@@ -171,6 +171,13 @@ __global__ void __launch_bounds__(128) k_heur_1opt(const Slot *slots, const int 
     if (h >= count) return;
     const int si = list[q];
     const Slot &s = slots[si];
+    // the node's problem: P0->n hyperplanes (heuristic.c:24-91) of its own order N
+    const int N = s.N;
+    const double *SL = s.SL;
+    if (h >= N) {
+        if (lane == 0) hval[(size_t)q * count + h] = -kBig;
+        return;
+    }
     const int n = s.n;
     const double *L = s.L;
     unsigned char *sg = signs + (size_t)q * sstride + (size_t)h * n;
@@ -299,10 +306,10 @@ void launch_heur_vectors(Slot *d, const int *slots, const unsigned long long *ke
     g = g > 64 ? 64 : g;
     k_heur_vec<<<dim3(g, nslots), 256, 0, st>>>(d, slots, keys, count, npad, stride, V);
 }
-void launch_heur_1opt(const Slot *d, const int *slots, int nslots, int count, int N, const int *lists, int list_stride,
-                      const double *SL, unsigned char *signs, size_t sstride, double *hval, cudaStream_t st) {
-    k_heur_1opt<<<dim3((count + 3) / 4, nslots), 128, 0, st>>>(d, slots, count, N, lists, list_stride, SL, signs,
-                                                                sstride, hval);
+void launch_heur_1opt(const Slot *d, const int *slots, int nslots, int count, const int *lists, int list_stride,
+                      unsigned char *signs, size_t sstride, double *hval, cudaStream_t st) {
+    k_heur_1opt<<<dim3((count + 3) / 4, nslots), 128, 0, st>>>(d, slots, count, lists, list_stride, signs, sstride,
+                                                                hval);
 }
 void launch_heur_signs(Slot *d, const int *slots, int nslots, int count, int npad, size_t stride, const float *H,
                        unsigned char *out, size_t out_stride, cudaStream_t st) {

@@ -140,10 +140,11 @@ __global__ void k_tri_reset(Slot *slots, TriSel *sel) {
 }
 
 // level 1 (level = 1) or level 2 (level = 2) bin selection, one thread per slot
-__global__ void k_tri_select(Slot *slots, TriSel *sel, int K, int level) {
+__global__ void k_tri_select(Slot *slots, TriSel *sel, int Kdefault, int level) {
     int b = blockIdx.x * blockDim.x + threadIdx.x;
     TriSel &T = sel[b];
     if (!slots[b].active) return;
+    const int K = slots[b].tri_k > 0 ? slots[b].tri_k : Kdefault;  // the slot's own problem's budget
     if (level == 1) {
         int total = 0;
         for (int q = 0; q < kHistBins; ++q) total += T.hist1[q];

@@ -10,10 +10,11 @@
 
 namespace mcb {
 
-__global__ void __launch_bounds__(256) k_subproblem(Slot *slots, const int *lists, int stride, const double *SL,
-                                                    int N, double *fixedval) {
+__global__ void __launch_bounds__(256) k_subproblem(Slot *slots, const int *lists, int stride, double *fixedval) {
     Slot &s = slots[blockIdx.x];
     if (!s.active) return;
+    const double *SL = s.SL;  // the slot's own problem
+    const int N = s.N;
     const int *ls = lists + (size_t)blockIdx.x * stride;
     const int nu = ls[0], nf1 = ls[1], nfx = ls[2];
     const int *U = ls + 3, *F1 = U + nu, *FX = F1 + nf1, *FS = FX + nfx;
@@ -68,9 +69,8 @@ __global__ void __launch_bounds__(256) k_subproblem(Slot *slots, const int *list
     if (threadIdx.x == 0) s.normL = sqrt(dg + 2.0 * lo);
 }
 
-void launch_subproblem(Slot *d, int ns, const int *d_lists, int list_stride, const double *d_SL, int N,
-                       double *d_fixed, cudaStream_t st) {
-    k_subproblem<<<ns, 256, 0, st>>>(d, d_lists, list_stride, d_SL, N, d_fixed);
+void launch_subproblem(Slot *d, int ns, const int *d_lists, int list_stride, double *d_fixed, cudaStream_t st) {
+    k_subproblem<<<ns, 256, 0, st>>>(d, d_lists, list_stride, d_fixed);
 }
 
 }  // namespace mcb

@@ -49,6 +49,7 @@ void launch_sa(Slot *d, void *jobs, int njobs, int *perm_scratch, int nmax, int 
 void sajob_fill(void *jobs_host, int idx, int slot, int k, int runs, int ntypes, uint64_t key, int out_off);
 
 // k_sub.cu
-void launch_subproblem(Slot *d, int ns, const int *d_lists, int list_stride, const double *d_SL, int N,
-                       double *d_fixed, cudaStream_t st);
+// createSubproblem (evaluate.c:39-116) for every active slot, from the slot's own
+// problem (Slot::SL, Slot::N) and its node lists
+void launch_subproblem(Slot *d, int ns, const int *d_lists, int list_stride, double *d_fixed, cudaStream_t st);
 }  // namespace mcb

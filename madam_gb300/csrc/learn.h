@@ -7,6 +7,6 @@ struct Slot;
 constexpr int kCutFeatures = 10;
 // F[q, :] = features of cut q (packed cps[8 q ..]) of slot slot_of[q], from that
 // slot's X and L; extra[q] = the cut's dual in the parent node (may be null)
-void launch_cut_features(const Slot *d_slots, const int *slot_of, const int *cps, int ncut, const double *extra, int N,
+void launch_cut_features(const Slot *d_slots, const int *slot_of, const int *cps, int ncut, const double *extra,
                          float *F, cudaStream_t st);
 }  // namespace mcb

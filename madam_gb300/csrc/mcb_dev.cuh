@@ -12,6 +12,9 @@ constexpr double kSaZero = 1e-11;   // |delta| below this is exactly zero in the
 // One node being bounded ("slot").  All matrices are n x n column-major with
 // leading dimension n, inside per-slot regions of Nmax*Nmax doubles.
 struct Slot {
+    const double *SL;  // the node's problem: SP->L (N x N, column-major) on the device
+    int N;        // the problem's order (the original variables plus the fixed last one)
+    int tri_k;    // triangle budget of the separation (TriIneq, twice that when the learned scorer ranks)
     int n;        // subproblem size
     int m;        // number of cuts (all families)
     int active;   // take part in the current launch

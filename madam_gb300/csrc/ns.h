@@ -137,7 +137,9 @@ void launch_heur_vectors(Slot *d, const int *slots, const unsigned long long *ke
 void launch_heur_xf(Slot *d, const int *slots, int nslots, int npad, size_t stride, float *Xf, cudaStream_t st);
 void launch_heur_signs(Slot *d, const int *slots, int nslots, int count, int npad, size_t stride, const float *H,
                        unsigned char *out, size_t out_stride, cudaStream_t st);
-// 1-opt from each hyperplane's signs (overwritten) and the cut value of the full solution
-void launch_heur_1opt(const Slot *d, const int *slots, int nslots, int count, int N, const int *lists, int list_stride,
-                      const double *SL, unsigned char *signs, size_t sstride, double *hval, cudaStream_t st);
+// 1-opt from each hyperplane's signs (overwritten) and the cut value of the full
+// solution, over the first N of the `count` hyperplanes of each listed slot (N the
+// order of the slot's own problem; the others get -inf)
+void launch_heur_1opt(const Slot *d, const int *slots, int nslots, int count, const int *lists, int list_stride,
+                      unsigned char *signs, size_t sstride, double *hval, cudaStream_t st);
 }  // namespace mcb

@@ -127,6 +127,12 @@ def lib():
     L.mcb_bab.argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_double), C.c_void_p, C.POINTER(C.c_double),
                           C.POINTER(C.c_int), C.c_void_p, C.c_int, C.POINTER(C.c_int)]
     L.mcb_set_time_limit.argtypes = [C.c_void_p, C.c_double]
+    L.mcb_add_problem.argtypes = [C.c_void_p, C.c_int, _dp]
+    L.mcb_problem_count.argtypes = [C.c_void_p]
+    L.mcb_bound_batch_multi.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p]
+    L.mcb_set_problem_lb.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_void_p]
+    L.mcb_get_problem_lb.restype = C.c_double
+    L.mcb_get_problem_lb.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
     L.mcb_set_cg_limit.argtypes = [C.c_void_p, C.c_int]
     L.mcb_tc_test_expiry.argtypes = [C.c_int]
     L.mcb_tc_test_expiry.restype = None
@@ -251,6 +257,35 @@ class Context:
         _check(lib().mcb_bound_batch(self.h, C.cast(arr, C.c_void_p), len(nodes), rank, b.ctypes.data,
                                      C.cast(sts, C.c_void_p)), self.h)
         return b, [sts[i] for i in range(len(nodes))]
+
+    def add_problem(self, SL, N):
+        """Another problem (SP->L of order N <= the context's) bounded by this context; its id."""
+        SLc = np.ascontiguousarray(np.asarray(SL, dtype=np.float64).reshape(-1))
+        rc = lib().mcb_add_problem(self.h, N, SLc)
+        if rc < 0:
+            _check(rc, self.h)
+        self._orders = getattr(self, "_orders", {0: self.N})
+        self._orders[rc] = N
+        return rc
+
+    def bound_batch_multi(self, nodes, problems, rank=1):
+        """Nodes of several problems in one batched pass (node i of problem problems[i])."""
+        arr = (C.POINTER(BabNode) * len(nodes))(*[C.pointer(nd) for nd in nodes])
+        pr = np.ascontiguousarray(problems, dtype=np.int32)
+        b = np.zeros(len(nodes))
+        sts = (NodeStats * len(nodes))()
+        _check(lib().mcb_bound_batch_multi(self.h, C.cast(arr, C.c_void_p), pr.ctypes.data, len(nodes), rank,
+                                           b.ctypes.data, C.cast(sts, C.c_void_p)), self.h)
+        return b, [sts[i] for i in range(len(nodes))]
+
+    def problem_lb(self, problem):
+        N = getattr(self, "_orders", {0: self.N}).get(problem, self.N)
+        s = np.zeros(N, dtype=np.int32)
+        v = lib().mcb_get_problem_lb(self.h, problem, s.ctypes.data)
+        return v, s[: N - 1]
+
+    def set_problem_lb(self, problem, lb):
+        _check(lib().mcb_set_problem_lb(self.h, problem, lb, None), self.h)
 
     def bab(self, batch=1, max_nodes=0, log_cap=100000):
         opt, rb = C.c_double(), C.c_double()
