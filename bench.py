@@ -15,7 +15,13 @@ second of the chosen form over the device-timed region (CUDA events on the
 library's stream); `e2e` is the same through the C ABI call with host buffers,
 timed on the host; `plain_fp64` is the plain form on the same workload in the
 same run, and `time_to_optimum` a full branch-and-bound of a seeded G(100, 0.5)
-unit-weight instance (triangle cuts) in both forms.
+unit-weight instance (triangle cuts) in both forms.  `n512` compares the forms on
+G(512, 0.1) with integer weights in [-10, 10] (node throughput, bound agreement,
+and a time-capped branch-and-bound of the whole graph); `uneven_batch` bounds the
+roots of 2000 seeded independent subproblems of uneven order in one call.  Both
+arms print the same `config` (the workload); the reference arm (`--impl
+reference`) runs the reference's method on the host cores, one process per core
+started before the timed steps.
 """
 import argparse
 import json
@@ -246,6 +252,44 @@ def n512_block(torch, M, stream, form, nodes=16, cap_s=60.0):
     return out
 
 
+def uneven_block(torch, M, stream, form, count=2000, plain_count=128, batch=128):
+    """The uneven batch: `count` seeded independent subproblems (n uniform in
+    [60, 400], density in [0.1, 0.9], weights +-1 or integers in [-10, 10]), their
+    root bounds in one call (mcb_bound_batch_multi; chunks of `batch` slots of
+    similar order) in the chosen form, the plain FP64 form on the first
+    `plain_count` of them, and the largest relative difference between the two
+    forms' bounds there."""
+    from madam_gb300 import workload as W
+
+    prm = M.params()
+    insts = [W.uneven_instance(sp) for sp in W.uneven_specs(count)]
+    out = {"subproblems": count, "n_range": [min(x[0] for x in insts), max(x[0] for x in insts)],
+           "slots": batch, "rank": 0, "params": "reference shipped params file (all three cut families)"}
+    res = {}
+    for f, k in ((form, count), ("fp64", plain_count)):
+        idx = list(range(k))
+        big = max(idx, key=lambda i: insts[i][0])  # problem 0 sizes the slots
+        ctx = _context(M, prm, insts[big][3], insts[big][0], batch, f, stream.cuda_stream, profile=False)
+        pid = {big: 0}
+        for i in idx:
+            if i != big:
+                pid[i] = ctx.add_problem(insts[i][3], insts[i][0])
+        nodes = [M.node({}) for _ in idx]
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        b, st = ctx.bound_batch_multi(nodes, [pid[i] for i in idx], rank=0)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        ctx.close()
+        res[f] = b
+        out[f] = {"value": k / dt, "unit": UNIT, "seconds": dt, "subproblems": k,
+                  "admm_iters": int(sum(x.admm_iters for x in st))}
+    rel = [abs(res[form][i] - res["fp64"][i]) / abs(res["fp64"][i]) for i in range(plain_count)]
+    out["bound_rel_diff_vs_fp64"] = {"max": max(rel), "mean": statistics.mean(rel), "over": plain_count}
+    out["speedup_vs_plain_fp64"] = out[form]["value"] / out["fp64"]["value"]
+    return out
+
+
 def _context(M, prm, SL, n, batch, form, stream=None, profile=True):
     flags = M.PROJ_FP64 if form == "fp64" else M.PROJ_NS_BF16
     if form == "learned":
@@ -393,7 +437,7 @@ def run_ours(a):
     roof = _roofline(M, ks, kw, a.workload)
     tot_ms = sum(x[1] for x in ks.values())
     share = {k: round(v[1] / max(1e-9, tot_ms), 4) for k, v in ks.items() if v[1] > 0}
-    plain = tto = n512 = None
+    plain = tto = n512 = uneven = None
     if not a.no_compare and a.form != "fp64":
         # the plain FP64 form on the same workload (one warm-up, one timed step)
         pc = _context(M, prm, wl["SL"], wl["n"], batch, "fp64", stream.cuda_stream, profile=False)
@@ -418,6 +462,7 @@ def run_ours(a):
         tto["same_optimum"] = tto["fp64"]["optimum"] == tto[a.form]["optimum"]
         if a.workload != N512:
             n512 = n512_block(torch, M, stream, a.form)
+        uneven = uneven_block(torch, M, stream, a.form)
     cpu = None
     if not a.no_cpu_baseline:
         cores = host_cores()
@@ -450,6 +495,7 @@ def run_ours(a):
         "speedup_vs_plain_fp64": (plain["ms_per_step"] / (dev_s * 1e3 / a.steps)) if plain else None,
         "time_to_optimum": tto,
         "n512": n512,
+        "uneven_batch": uneven,
         "cpu_baseline": cpu,
         "clocks": clk,
     }
