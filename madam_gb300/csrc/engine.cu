@@ -969,7 +969,7 @@ uint64_t node_key(const int *xfixed, const int *sol, int pb) {
 }
 
 // Newton-Schulz form: the heuristic's hyperplane signs sign(X v) for every node in
-// hrun, computed on the GPU (one TF32 GEMM per node) and copied to r.signs
+// hrun, computed on the GPU (the library's tcgen05 GEMM) and copied to r.signs
 int ns_hyperplanes(mcb_ctx *c, std::vector<NodeRun *> &runs, std::vector<NodeRun *> &hrun) {
     std::vector<int> list;
     std::vector<unsigned long long> keys;
@@ -993,8 +993,10 @@ int ns_hyperplanes(mcb_ctx *c, std::vector<NodeRun *> &runs, std::vector<NodeRun
     CUDA_TRY(c, h2d(c, c->d_hkeys, keys.data(), k * sizeof(unsigned long long)));
     int rc;
     {
-        Prof p(c, K_HEUR, 3);
-        c->lib_launches += 1;
+        // tcgen05 path: X, the normals, their planes, the product and the signs;
+        // the cuBLAS operand modes take a cuBLAS GEMM (counted apart) instead
+        Prof p(c, K_HEUR, c->ns.tc() ? 6 : 3);
+        if (!c->ns.tc()) c->lib_launches += 1;
         rc = c->ns.hyperplanes(c->d_slots, list, c->d_hlist, c->d_hkeys, count, (nm + 15) / 16 * 16, c->d_hsign,
                                ostride, c->st);
     }

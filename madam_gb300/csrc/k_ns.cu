@@ -120,18 +120,19 @@ __global__ void __launch_bounds__(256) k_heur_xf(Slot *slots, const int *list, i
 }
 
 // V[:, c] = the n draws (uniform in [-0.5, 0.5)) of stream key2(key, c): draw i of a
-// counter stream is mix64(key + (i + 1) * golden), see Stream::next
+// counter stream is mix64(key + (i + 1) * golden), see Stream::next; columns
+// count .. rows - 1 are zero
 __global__ void __launch_bounds__(256) k_heur_vec(Slot *slots, const int *list, const unsigned long long *keys,
-                                                  int count, int npad, size_t stride, float *V) {
+                                                  int count, int rows, int npad, size_t stride, float *V) {
     const int si = list[blockIdx.y];
     const int n = slots[si].n;
     const uint64_t key = keys[blockIdx.y];
     float *Vb = V + (size_t)si * stride;
-    const size_t tot = (size_t)npad * count;
+    const size_t tot = (size_t)npad * rows;
     for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < tot; q += (size_t)gridDim.x * blockDim.x) {
         int c = (int)(q / npad), i = (int)(q - (size_t)c * npad);
         float v = 0.0f;
-        if (i < n) {
+        if (i < n && c < count) {
             uint64_t kc = key2(key, (uint64_t)c);
             uint64_t z = mix64(kc + (uint64_t)(i + 1) * 0x9E3779B97F4A7C15ull);
             v = (float)((double)(z >> 11) * 0x1.0p-53 - 0.5);
@@ -300,11 +301,11 @@ void launch_heur_xf(Slot *d, const int *slots, int nslots, int npad, size_t stri
     g = g > 64 ? 64 : g;
     k_heur_xf<<<dim3(g, nslots), 256, 0, st>>>(d, slots, npad, stride, Xf);
 }
-void launch_heur_vectors(Slot *d, const int *slots, const unsigned long long *keys, int nslots, int count, int npad,
-                         size_t stride, float *V, cudaStream_t st) {
-    int g = grid_for((size_t)npad * count);
+void launch_heur_vectors(Slot *d, const int *slots, const unsigned long long *keys, int nslots, int count, int rows,
+                         int npad, size_t stride, float *V, cudaStream_t st) {
+    int g = grid_for((size_t)npad * rows);
     g = g > 64 ? 64 : g;
-    k_heur_vec<<<dim3(g, nslots), 256, 0, st>>>(d, slots, keys, count, npad, stride, V);
+    k_heur_vec<<<dim3(g, nslots), 256, 0, st>>>(d, slots, keys, count, rows, npad, stride, V);
 }
 void launch_heur_1opt(const Slot *d, const int *slots, int nslots, int count, const int *lists, int list_stride,
                       unsigned char *signs, size_t sstride, double *hval, cudaStream_t st) {
@@ -613,12 +614,38 @@ int NsProj::hyperplanes(Slot *d_slots, const std::vector<int> &slots, const int 
         hptr[1 * cap + q] = T + o;   // hyperplane normals
         hptr[2 * cap + q] = S2 + o;  // X V
     }
+    if (tc()) {
+        // H = V X on the library's tcgen05 kernel: the normals (rows of V, zero rows
+        // past `count`) and X as digit planes in the projection's plane buffers,
+        // both padded to a multiple of 128 that holds the subproblem and the count
+        const int np2 = (std::max(npad_, count) + 127) / 128 * 128;
+        const size_t tot = stride * (size_t)cap;
+        launch_heur_xf(d_slots, d_list, k, np2, stride, S, st);
+        launch_heur_vectors(d_slots, d_list, d_keys, k, count, np2, np2, stride, T, st);
+        // |X_ij| <= 1 for the ADMM's X (unit diagonal, PSD) up to its tolerance: sigma = 4;
+        // the normals lie in [-1/2, 1/2): sigma = 1
+        TcOut ox = planes_out(Sp, tot, stride, nullptr, 32.0f), ov = planes_out(Tp, tot, stride, nullptr, 128.0f);
+        tc_split_f32(S, stride, ox, np2, k, d_list, st);
+        tc_split_f32(T, stride, ov, np2, k, d_list, st);
+        alignas(64) unsigned char hm[2 * kTcPieces][128];
+        for (int p = 0; p < kTcPieces; ++p) {
+            if (int rc = tc_make_map(hm[p], ov.p[p], np2, stride, cap)) return rc;
+            if (int rc = tc_make_map(hm[kTcPieces + p], ox.p[p], np2, stride, cap)) return rc;
+        }
+        map_npad = 0;  // the projection's maps are rebuilt at its next set_live
+        TcOut oh{S2, nullptr, {}, stride, d_err, 1.0f, nullptr};
+        // row c of the product is X v_c (X is symmetric); no diagonal term
+        if (int rc = tc_gemm(hm[0], hm[kTcPieces], oh, np2, k, d_list, d_n, 1.0f, 0.0f, 4.0f / 16384.0f, st, 0, 0))
+            return rc;
+        launch_heur_signs(d_slots, d_list, k, count, np2, stride, S2, d_out, out_stride, st);
+        return MCB_OK;
+    }
     if (cudaMemcpyAsync(dptr, hptr.data(), 3 * (size_t)cap * sizeof(void *), cudaMemcpyHostToDevice, st) != cudaSuccess)
         return MCB_ERR_CUDA;
     if (cudaStreamSynchronize(st) != cudaSuccess) return MCB_ERR_CUDA;
     live = 0;  // the live-slot arrays were overwritten
     launch_heur_xf(d_slots, d_list, k, npad_, stride, S, st);
-    launch_heur_vectors(d_slots, d_list, d_keys, k, count, npad_, stride, T, st);
+    launch_heur_vectors(d_slots, d_list, d_keys, k, count, count, npad_, stride, T, st);
     cublasSetStream(h, st);
     const float one = 1.0f, zero = 0.0f;
     if (cublasGemmBatchedEx(h, CUBLAS_OP_N, CUBLAS_OP_N, npad_, count, npad_, &one, (const void *const *)dptr,

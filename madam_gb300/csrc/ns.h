@@ -132,7 +132,7 @@ void launch_ns_post0(Slot *d, int ns, int nmax, const double *G, int npad, size_
 // hyperplane rounding of the heuristic on the GPU: signs of X v for `count`
 // counter-stream vectors v per slot (the vectors of the plain form's host
 // heuristic, drawn in dimension n); out: n x count bytes per slot, 1 = negative
-void launch_heur_vectors(Slot *d, const int *slots, const unsigned long long *keys, int nslots, int count,
+void launch_heur_vectors(Slot *d, const int *slots, const unsigned long long *keys, int nslots, int count, int rows,
                          int npad, size_t stride, float *V, cudaStream_t st);
 void launch_heur_xf(Slot *d, const int *slots, int nslots, int npad, size_t stride, float *Xf, cudaStream_t st);
 void launch_heur_signs(Slot *d, const int *slots, int nslots, int count, int npad, size_t stride, const float *H,
