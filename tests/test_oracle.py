@@ -71,6 +71,39 @@ def test_oracle_reproduces_reference_trees_under_other_parameters(orc, fx):
     assert max(abs(a - b) for a, b in zip(bounds, fx["bounds"])) <= 1e-9
 
 
+def test_oracle_stream_modes_agree_where_no_stream_is_drawn(orc):
+    """The GPU form reproduces the oracle's counter-stream mode; the oracle's glibc
+    mode (the reference's rand() streams, top-K order and eigenvector signs) is
+    pinned bit-exact to the reference.  Where no random draw can matter -- triangle
+    cuts only (no simulated annealing) and the incumbent fixed at the optimum (the
+    rounding heuristic cannot change it, so pruning and give-ups see the same value)
+    -- the two modes must give the same counts, and bounds equal up to rounding
+    (the modes store the same cut set in different orders -- scan order against the
+    reference's replacement order -- so their sums round differently; ~1e-9 here),
+    which closes the chain GPU = oracle(counter) = oracle(glibc) = reference on that
+    path."""
+    fx = [f for f in VARIANTS if f["name"] == "gnp56_pm1_s31_tri"][0]
+    n, e, w = _fixture_instance(fx)
+    SL = orc.build_L(n, (e, w))
+    prm = orc.shipped_params(**dict(fx["params"], use_diff=0))
+    rng = np.random.default_rng(3)
+    fixings = [{}] + [{int(v): int(rng.integers(0, 2)) for v in rng.choice(n - 1, size=k, replace=False)}
+                      for k in (2, 5, 9)]
+    ran = 0
+    for fixed in fixings:
+        out = []
+        for mode in ((orc.RNG_COUNTER, orc.TOPK_CANONICAL, 1), (orc.RNG_GLIBC, orc.TOPK_REFERENCE, 0)):
+            c = orc.Ctx(prm, SL, n, rng=mode[0], topk=mode[1], canon_sign=mode[2])
+            c.set_lb(fx["opt"])
+            b, st = c.evaluate(orc.make_node(n - 1, fixed), rank=1)
+            out.append((b, st.admm_iters, st.outer_iters, st.n_tri))
+            c.close()
+        (b0, *k0), (b1, *k1) = out
+        assert k0 == k1 and abs(b0 - b1) <= 1e-7 * abs(b1), (fixed, out)
+        ran += k0[0] > 0
+    assert ran >= 3  # the cutting-plane rounds ran on most of the nodes
+
+
 def test_oracle_counter_mode_is_order_free(orc):
     """Counter streams: a node's bound does not depend on what was bounded before."""
     n, e, w = G.gnp(36, 0.5, "pm1", seed=21)
