@@ -62,6 +62,8 @@ struct SlotMem {
     double *cutd = nullptr;  // 8 * mcap: t s u v rhs cgr cgp cgq
     int *g_rp = nullptr, *g_ci = nullptr;
     double *g_v = nullptr;
+    float *g_v32 = nullptr;
+    size_t g32cap = 0;
     int *e_idx = nullptr, *e_rp = nullptr, *e_cut = nullptr;
     double *e_coef = nullptr;
 };
@@ -322,19 +324,26 @@ int ensure_cut_capacity(mcb_ctx *c, int si, int m, size_t nnz_g, size_t ne, size
         M.mcap = nc;
     }
     if ((rc = grow2(c, M.g_ci, M.g_v, M.gcap, nnz_g))) return rc;
+    if (nnz_g > M.g32cap || !M.g_v32) {
+        if (M.g_v32) cudaFree(M.g_v32);
+        M.g_v32 = nullptr;
+        CUDA_TRY(c, cudaMalloc(&M.g_v32, M.gcap * sizeof(float)));
+        M.g32cap = M.gcap;
+    }
     if ((rc = grow2(c, M.e_idx, M.e_rp, M.eicap, ne + 1, 1))) return rc;
     if ((rc = grow2(c, M.e_cut, M.e_coef, M.ecap, nnz_e + 1))) return rc;
     size_t mc = M.mcap;
     s.cp = M.cp;
     s.t = M.cutd; s.s = M.cutd + mc; s.u = M.cutd + 2 * mc; s.v = M.cutd + 3 * mc;
     s.rhs = M.cutd + 4 * mc; s.cgr = M.cutd + 5 * mc; s.cgp = M.cutd + 6 * mc; s.cgq = M.cutd + 7 * mc;
-    s.g_rp = M.g_rp; s.g_ci = M.g_ci; s.g_v = M.g_v;
+    s.g_rp = M.g_rp; s.g_ci = M.g_ci; s.g_v = M.g_v; s.g_v32 = M.g_v32;
     s.e_idx = M.e_idx; s.e_rp = M.e_rp; s.e_cut = M.e_cut; s.e_coef = M.e_coef;
     return MCB_OK;
 }
 
 void free_slot(SlotMem &M) {
-    void *ps[] = {M.mats, M.vecs, M.acc, M.dwork, M.cp, M.cutd, M.g_rp, M.g_ci, M.g_v, M.e_idx, M.e_rp, M.e_cut, M.e_coef};
+    void *ps[] = {M.mats, M.vecs, M.acc, M.dwork, M.cp, M.cutd, M.g_rp, M.g_ci, M.g_v, M.g_v32, M.e_idx, M.e_rp, M.e_cut,
+                  M.e_coef};
     for (void *p : ps)
         if (p) cudaFree(p);
     M = SlotMem();
@@ -1260,6 +1269,7 @@ int bound_batch(mcb_ctx *c, mcb_bab_node *const *nodes, const int *probs, int co
             emax = std::max(emax, s.ne);
         }
         if ((rc = upload_slots(c, ns))) return rc;
+        launch_cg_values(c->d_slots, ns, c->st);  // FP32 copy of B B^T + I for the inner CG
         tick(H_CUTS);
         // ADMM_solver (admm.c:49-771): chunks of iterations until every live slot stopped
         for (int it = 0; it < P.ADMM_itermax + 8;) {

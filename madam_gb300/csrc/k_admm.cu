@@ -60,62 +60,96 @@ __global__ void k_admm_rhs(Slot *slots) {
     }
 }
 
-// (B B^T + I) t = rhs by conjugate gradients, warm-started from the current t,
-// to ||r|| <= rtol ||rhs|| (the reference factors with CHOLMOD, admm.c:546; the
-// plain form uses rtol = 1e-13).  One CTA per slot.  An iteration cap sets
-// status and leaves t as is.
+// (B B^T + I) t = rhs (the reference factors with CHOLMOD, admm.c:546) to
+// ||rhs - A t|| <= rtol ||rhs|| (the plain form uses rtol = 1e-13), warm-started
+// from the current t, by mixed-precision iterative refinement: the true residual
+// r = rhs - A t and the stopping test in FP64, the correction A d = r by
+// conjugate gradients in FP32 (its rate is ~64x FP64's on this part) to 1e-5 of
+// ||r||, then t += d.  A has eigenvalues in [1, ~11], so each outer step gains
+// about five digits and two or three reach 1e-13.  One CTA per slot; the FP32
+// work arrays reuse cgp and cgq (two floats per double), the FP32 copy of A's
+// values is g_v32.  The iteration cap counts the FP32 CG iterations; reaching it
+// before the tolerance sets status and leaves t as far as it got.
+constexpr int kCgOuter = 12;           // refinement steps at most
+constexpr double kCgInnerRel2 = 1e-10;  // (1e-5)^2: the inner CG's relative target
 __global__ void __launch_bounds__(1024) k_cg(Slot *slots, int maxit, double rtol2) {
     Slot &s = slots[blockIdx.x];
     if (!live(s)) return;
     const int m = s.m;
     if (m == 0) return;
     __shared__ double red[40];
-    double *x = s.t, *r = s.cgr, *p = s.cgp, *q = s.cgq;
+    double *x = s.t, *r = s.cgr;
+    float *d = (float *)s.cgp, *ri = d + m, *p = (float *)s.cgq, *q = p + m;
     const int *rp = s.g_rp, *ci = s.g_ci;
     const double *gv = s.g_v;
-    double lbb = 0.0, lrr = 0.0;
-    for (int i = threadIdx.x; i < m; i += blockDim.x) {
-        double acc = 0.0;
-        for (int k = rp[i]; k < rp[i + 1]; ++k) acc += gv[k] * x[ci[k]];
-        double b = s.rhs[i];
-        double ri = b - acc;
-        r[i] = ri;
-        p[i] = ri;
-        lbb += b * b;
-        lrr += ri * ri;
-    }
-    double bb = block_sum(lbb, red);
-    double rr = block_sum(lrr, red);
+    const float *gf = s.g_v32;
+    double lbb = 0.0;
+    for (int i = threadIdx.x; i < m; i += blockDim.x) lbb += s.rhs[i] * s.rhs[i];
+    const double bb = block_sum(lbb, red);
     const double stop2 = rtol2 * bb;
     int it = 0;
-    while (rr > stop2 && it < maxit) {
-        double lpq = 0.0;
+    double rr = 0.0;
+    for (int outer = 0;; ++outer) {
+        double lrr = 0.0;
         for (int i = threadIdx.x; i < m; i += blockDim.x) {
             double acc = 0.0;
-            for (int k = rp[i]; k < rp[i + 1]; ++k) acc += gv[k] * p[ci[k]];
-            q[i] = acc;
-            lpq += p[i] * acc;
+            for (int k = rp[i]; k < rp[i + 1]; ++k) acc += gv[k] * x[ci[k]];
+            const double res = s.rhs[i] - acc;
+            r[i] = res;
+            lrr += res * res;
         }
-        double pq = block_sum(lpq, red);
-        double alpha = rr / pq;
-        double l2 = 0.0;
+        rr = block_sum(lrr, red);
+        if (rr <= stop2 || it >= maxit || outer >= kCgOuter) break;
+        // the correction, on the residual scaled to unit norm (FP32's range)
+        const double nr = sqrt(rr), inv = 1.0 / nr;
         for (int i = threadIdx.x; i < m; i += blockDim.x) {
-            x[i] += alpha * p[i];
-            double ri = r[i] - alpha * q[i];
-            r[i] = ri;
-            l2 += ri * ri;
+            const float v = (float)(r[i] * inv);
+            ri[i] = v;
+            p[i] = v;
+            d[i] = 0.0f;
         }
-        double rr2 = block_sum(l2, red);
-        double beta = rr2 / rr;
-        for (int i = threadIdx.x; i < m; i += blockDim.x) p[i] = r[i] + beta * p[i];
         __syncthreads();
-        rr = rr2;
-        ++it;
+        double rz = 1.0;  // the scaled residual's squared norm
+        while (rz > kCgInnerRel2 && it < maxit) {
+            double lpq = 0.0;
+            for (int i = threadIdx.x; i < m; i += blockDim.x) {
+                float acc = 0.0f;
+                for (int k = rp[i]; k < rp[i + 1]; ++k) acc = fmaf(gf[k], p[ci[k]], acc);
+                q[i] = acc;
+                lpq += (double)(p[i] * acc);
+            }
+            const double pq = block_sum(lpq, red);
+            const float alpha = (float)(rz / pq);
+            double l2 = 0.0;
+            for (int i = threadIdx.x; i < m; i += blockDim.x) {
+                d[i] = fmaf(alpha, p[i], d[i]);
+                const float v = fmaf(-alpha, q[i], ri[i]);
+                ri[i] = v;
+                l2 += (double)(v * v);
+            }
+            const double rz2 = block_sum(l2, red);
+            const float beta = (float)(rz2 / rz);
+            for (int i = threadIdx.x; i < m; i += blockDim.x) p[i] = fmaf(beta, p[i], ri[i]);
+            __syncthreads();
+            rz = rz2;
+            ++it;
+        }
+        for (int i = threadIdx.x; i < m; i += blockDim.x) x[i] += nr * (double)d[i];
+        __syncthreads();
     }
     if (threadIdx.x == 0) {
         s.cg_iters = it;
-        if (it >= maxit && rr > stop2) s.status = -6;
+        if (rr > stop2) s.status = -6;
     }
+}
+
+// the FP32 copy of A's values for the inner CG (k_cg), per live slot
+__global__ void k_cg_values(Slot *slots) {
+    Slot &s = slots[blockIdx.y];
+    if (!s.active) return;
+    const int nnz = s.m > 0 ? s.g_rp[s.m] : 0;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nnz; k += gridDim.x * blockDim.x)
+        s.g_v32[k] = (float)s.g_v[k];
 }
 
 // admm.c:556-560, 587-591: v = t - u/sigma, s = v_+, u = -sigma v_- ; and W (admm.c:564-568):
@@ -294,6 +328,7 @@ void launch_admm_rhs(Slot *d, int ns, int nmax, int mmax, cudaStream_t st) {
 void launch_cg(Slot *d, int ns, int maxit, double rtol, cudaStream_t st) {
     k_cg<<<ns, 1024, 0, st>>>(d, maxit, rtol * rtol);
 }
+void launch_cg_values(Slot *d, int ns, cudaStream_t st) { k_cg_values<<<dim3(64, ns), 256, 0, st>>>(d); }
 void launch_admm_su(Slot *d, int ns, int mmax, cudaStream_t st) {
     dim3 g(cdiv(mmax > 1 ? mmax : 1, 256) < 512 ? cdiv(mmax > 1 ? mmax : 1, 256) : 512, ns);
     k_admm_su<<<g, 256, 0, st>>>(d);

@@ -38,6 +38,7 @@ struct Slot {
     // (B B^T + I) in CSR
     int *g_rp, *g_ci;
     double *g_v;
+    float *g_v32;  // the values in FP32 (the inner CG)
     // B^T incidence: ne distinct lower elements e_idx[q] = i + j n (i > j), each with
     // the list e_rp[q]..e_rp[q+1] of (cut, coefficient) in cut order
     int ne;
