@@ -6,6 +6,8 @@
 // by inverse iteration with re-orthogonalisation inside clusters (dstein), then
 // back-transforms (dormtr).  These kernels do the same four steps on the GPU,
 // one CTA per node, FP64 throughout, with full-precision bisection.
+#include <cooperative_groups.h>
+
 #include "mcb_dev.cuh"
 #include "ns.h"
 #include "kernels.h"
@@ -85,6 +87,103 @@ __global__ void __launch_bounds__(512) k_tridiag(Slot *slots, int gate) {
         __syncthreads();
     }
     if (tid == 0) {
+        if (n >= 2) {
+            s.d[n - 2] = A[(n - 2) + (size_t)(n - 2) * n];
+            s.d[n - 1] = A[(n - 1) + (size_t)(n - 1) * n];
+            s.e[n - 2] = A[(n - 1) + (size_t)(n - 2) * n];
+            s.tau[n - 2] = 0.0;
+        } else if (n == 1) {
+            s.d[0] = A[0];
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// The same reduction with a slot's rows spread over the C CTAs of a thread-block
+// cluster (C = gridDim.x), so that a node's 4/3 n^3 FP64 flops run on C SMs'
+// FP64 pipes.  At step k the trailing rows k+1+i, i in [0, m), are dealt in chunks
+// of ceil(m / C): CTA c owns chunk c (CTA 0 always owns i = 0) and reads and writes
+// only its own rows of A, so the symmetric product w = tau A22 v and the rank-2
+// update need no exchange of matrix data.  The exchanges go through the slot's
+// work array s.dwork (w, and per-CTA partial sums added in CTA order, so every CTA
+// gets the same sigma^2 and v^T w), with two cluster barriers per step (release /
+// acquire at cluster scope): after the sigma^2 partials (which also publishes the
+// previous step's update of column k) and after w.  Every CTA of a cluster runs
+// the same loop with the same barrier sequence (the slot, n and tau are common to
+// the cluster), so the barriers always match.
+__global__ void __launch_bounds__(512) k_tridiag_cl(Slot *slots, int gate) {
+    Slot &s = slots[blockIdx.y];
+    if (!gated(s, gate)) return;  // common to the cluster: the CTAs of one slot
+    namespace cg = cooperative_groups;
+    cg::cluster_group cl = cg::this_cluster();
+    const int n = s.n, tid = threadIdx.x, bs = blockDim.x;
+    const int C = gridDim.x, c = blockIdx.x;
+    double *A = s.A;
+    extern __shared__ double sh[];
+    double *v = sh, *w = sh + n, *red = sh + 2 * n;
+    double *gw = s.dwork, *gp = s.dwork + n;  // w; partials: [0, C) sigma^2, [C, 2C) v^T w
+    for (int k = 0; k < n - 2; ++k) {
+        const int m = n - k - 1;
+        const int chunk = (m + C - 1) / C, i0 = min(m, c * chunk), i1 = min(m, i0 + chunk);
+        double *x = A + (k + 1) + (size_t)k * n;
+        double loc = 0.0;
+        for (int i = max(i0, 1) + tid; i < i1; i += bs) loc += x[i] * x[i];
+        loc = block_sum(loc, red);
+        if (tid == 0) gp[c] = loc;
+        cl.sync();
+        double sig2 = 0.0;
+        for (int q = 0; q < C; ++q) sig2 += gp[q];
+        const double alpha = x[0];
+        double beta, tau, scal;
+        if (sig2 == 0.0) {
+            beta = alpha;
+            tau = 0.0;
+            scal = 0.0;
+        } else {
+            beta = -copysign(sqrt(alpha * alpha + sig2), alpha);
+            tau = (beta - alpha) / beta;
+            scal = 1.0 / (alpha - beta);
+        }
+        for (int i = tid; i < m; i += bs) v[i] = i == 0 ? 1.0 : x[i] * scal;
+        __syncthreads();
+        if (tau != 0.0) {
+            const double *A22 = A + (k + 1) + (size_t)(k + 1) * n;
+            double lp = 0.0;
+            for (int i = i0 + tid; i < i1; i += bs) {
+                double acc = 0.0;
+                for (int j = 0; j < m; ++j) acc += A22[i + (size_t)j * n] * v[j];
+                const double wi = tau * acc;
+                gw[i] = wi;
+                lp += wi * v[i];
+            }
+            lp = block_sum(lp, red);
+            if (tid == 0) gp[C + c] = lp;
+        }
+        cl.sync();
+        // every CTA has read column k: store the reflector in its own rows
+        for (int i = max(i0, 1) + tid; i < i1; i += bs) x[i] = v[i];
+        if (c == 0 && tid == 0) {
+            s.d[k] = A[k + (size_t)k * n];
+            s.e[k] = beta;
+            s.tau[k] = tau;
+        }
+        if (tau != 0.0) {
+            double pv = 0.0;
+            for (int q = 0; q < C; ++q) pv += gp[C + q];
+            const double K = -0.5 * tau * pv;
+            for (int i = tid; i < m; i += bs) w[i] = gw[i] + K * v[i];
+            __syncthreads();
+            double *U = A + (k + 1) + (size_t)(k + 1) * n;
+            const int rows = i1 - i0;
+            for (int idx = tid; idx < rows * m; idx += bs) {
+                const int j = idx / rows, i = i0 + idx - j * rows;
+                U[i + (size_t)j * n] -= v[i] * w[j] + w[i] * v[j];
+            }
+        }
+        __syncthreads();
+    }
+    cl.sync();
+    if (c == 0 && tid == 0) {
         if (n >= 2) {
             s.d[n - 2] = A[(n - 2) + (size_t)(n - 2) * n];
             s.d[n - 1] = A[(n - 1) + (size_t)(n - 1) * n];
@@ -543,7 +642,25 @@ void launch_sym_copy(Slot *d_slots, int nslots, int nmax, int src, int gate, cud
 }
 void launch_tridiag(Slot *d_slots, int nslots, int nmax, int gate, cudaStream_t st) {
     size_t sm = (2 * (size_t)nmax + 40) * sizeof(double);
-    k_tridiag<<<nslots, 512, sm, st>>>(d_slots, gate);
+    // a cluster of C CTAs per slot (about 64 rows per CTA, at most the portable 8)
+    const int C = nmax >= 384 ? 8 : (nmax >= 192 ? 4 : (nmax >= 96 ? 2 : 1));
+    if (C == 1) {
+        k_tridiag<<<nslots, 512, sm, st>>>(d_slots, gate);
+        return;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(C, nslots);
+    cfg.blockDim = dim3(512);
+    cfg.dynamicSmemBytes = sm;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = C;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, k_tridiag_cl, d_slots, gate);
 }
 void launch_bisect(Slot *d_slots, int nslots, int nmax, double vl, int largest_only, int gate,
                    cudaStream_t st) {
