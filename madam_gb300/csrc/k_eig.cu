@@ -465,11 +465,16 @@ __global__ void __launch_bounds__(64) k_invit(Slot *slots, int gate) {
 
 // ---------------------------------------------------------------------------
 // V (n x M) <- Q V with Q = H_0 H_1 ... H_{n-3} (dormtr).
+// The columns of V are independent: CTA blockIdx.x takes columns
+// [kBtCols blockIdx.x, kBtCols (blockIdx.x + 1)) of its slot, so that a node's
+// 2 n^2 M FP64 flops spread over several SMs.
+constexpr int kBtCols = 32;
 __global__ void __launch_bounds__(256) k_backtrans(Slot *slots, int gate) {
-    Slot &s = slots[blockIdx.x];
+    Slot &s = slots[blockIdx.y];
     if (!gated(s, gate)) return;
     const int n = s.n, M = s.M, lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    if (M <= 0 || n < 3) return;
+    const int c0 = blockIdx.x * kBtCols, c1 = min(M, c0 + kBtCols), nc = c1 - c0;
+    if (nc <= 0 || n < 3) return;
     extern __shared__ double sh[];
     double *v = sh, *sc = sh + n;
     const double *A = s.A;
@@ -480,17 +485,17 @@ __global__ void __launch_bounds__(256) k_backtrans(Slot *slots, int gate) {
         const int m = n - k - 1;
         for (int i = threadIdx.x; i < m; i += blockDim.x) v[i] = i == 0 ? 1.0 : A[(k + 1 + i) + (size_t)k * n];
         __syncthreads();
-        for (int c = wid; c < M; c += nw) {
+        for (int c = c0 + wid; c < c1; c += nw) {
             const double *col = V + (size_t)c * n + k + 1;
             double acc = 0.0;
             for (int i = lane; i < m; i += 32) acc += v[i] * col[i];
             acc = warp_sum(acc);
-            if (lane == 0) sc[c] = tau * acc;
+            if (lane == 0) sc[c - c0] = tau * acc;
         }
         __syncthreads();
-        for (int idx = threadIdx.x; idx < m * M; idx += blockDim.x) {
+        for (int idx = threadIdx.x; idx < m * nc; idx += blockDim.x) {
             int c = idx / m, i = idx - c * m;
-            V[(size_t)c * n + k + 1 + i] -= sc[c] * v[i];
+            V[(size_t)(c0 + c) * n + k + 1 + i] -= sc[c] * v[i];
         }
         __syncthreads();
     }
@@ -676,7 +681,7 @@ void launch_invit(Slot *d_slots, int nslots, int nmax, int gate, cudaStream_t st
 }
 void launch_backtrans(Slot *d_slots, int nslots, int nmax, int gate, cudaStream_t st) {
     size_t sm = (2 * (size_t)nmax) * sizeof(double);
-    k_backtrans<<<nslots, 256, sm, st>>>(d_slots, gate);
+    k_backtrans<<<dim3((nmax + kBtCols - 1) / kBtCols, nslots), 256, sm, st>>>(d_slots, gate);
 }
 void launch_canon_scale(Slot *d_slots, int nslots, int nmax, int gate, cudaStream_t st) {
     dim3 g((nmax + 7) / 8, nslots);
