@@ -35,7 +35,7 @@ def main(out=OUT, epochs=60):
     parts = []
     for (kind, *args), seeds, over, cap in SOURCES:
         inst = [L.instance(kind, *args, seed=s) for s in seeds]
-        parts.append(L.collect(inst, proj=M.PROJ_NS_BF16, batch=8, max_nodes=cap, params=over))
+        parts.append(L.collect(inst, proj=M.PROJ_FP64, batch=8, max_nodes=cap, params=over))
     Xs = np.concatenate([p[0] for p in parts]); ys = np.concatenate([p[1] for p in parts])
     Xw = np.concatenate([p[2] for p in parts]); yw = np.concatenate([p[3] for p in parts])
     scorer, ls = L.train(Xs, ys, epochs=epochs, seed=1)

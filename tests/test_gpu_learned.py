@@ -18,7 +18,7 @@ PRM = dict(include_Pent=0, include_Hepta=0)
 @pytest.fixture(scope="module")
 def models(gpu_lib):
     inst = [L.instance("gnp", 90, 0.5, "one", seed=s) for s in (31, 32)]
-    Xs, ys, Xw, yw = L.collect(inst, proj=gpu_lib.PROJ_NS_BF16, batch=8, max_nodes=120, params=PRM)
+    Xs, ys, Xw, yw = L.collect(inst, proj=gpu_lib.PROJ_FP64, batch=8, max_nodes=120, params=PRM)
     assert len(ys) > 1000 and len(yw) > 1000
     assert np.all(ys >= 0) and np.all(yw >= 0)
     scorer, ls = L.train(Xs, ys, epochs=40, seed=1)
