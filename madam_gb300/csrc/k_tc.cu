@@ -25,17 +25,21 @@
 // which is slow on this part) and writes C as FP32, as FP64 (times a per-slot
 // factor) and/or as the next step's five digit planes.
 //
-// Tiling: one CTA per 128 x 128 tile of C and slot; K in chunks of 32 BF16 (one
-// 64-byte swizzle row).  A stage holds the five planes of the A and B chunks
-// (80 KB).  The four accumulators take all 512 tensor-memory columns, so one CTA
-// runs per SM; the autotuner times two variants: two pipeline stages (TMA of the
-// next chunk under the MMAs of this one) or one.  One thread issues the TMA copies
-// and the MMAs; all four warps drain the accumulators (32 lanes each) with
-// tcgen05.ld, through shared-memory tiles (row-major for the direct half,
-// column-major for the mirror, 64 columns at a time) so that every global store
-// is coalesced.  Every wait on an mbarrier is bounded: on expiry the CTA records
-// an error code, gives the TMA loads it still has in flight their own bounded
-// wait, skips the rest and releases its tensor memory.
+// Tiling: one CTA of eight warps per 128 x 128 tile of C and slot; K in chunks of
+// 32 BF16 (one 64-byte swizzle row).  A stage holds the five planes of the A and
+// B chunks (80 KB).  The four accumulators take all 512 tensor-memory columns, so
+// one CTA runs per SM; the autotuner times two variants: two pipeline stages or
+// one.  One thread of warp 1 issues the TMA copies (waiting only for a stage to be
+// released), one thread of warp 0 issues the MMAs (waiting only for a stage to
+// land), so the MMAs of the next chunk queue behind those of this one.  All eight
+// warps drain the accumulators with tcgen05.ld (warp w: lanes 32 (w mod 4) .. +31,
+// columns 64 (w / 4) .. +63), each element once: its float-pair value, digit
+// planes and FP32 / FP64 forms are made in registers and stored to the element's
+// place (16 consecutive columns of a row per thread, vector stores of whole
+// 32-byte sectors) and to its mirror (one element per lane, consecutive across
+// the warp).  Every wait on an mbarrier is bounded: on expiry the CTA records an
+// error code, gives the TMA loads it still has in flight their own bounded wait,
+// skips the rest and releases its tensor memory.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -55,10 +59,8 @@ constexpr int BM = 128, BN = 128, BK = 32;
 constexpr int kPieces = kTcPieces;
 constexpr int kTileBytes = BM * BK * 2;                // one plane of one operand chunk (8 KB)
 constexpr int kStageBytes = 2 * kPieces * kTileBytes;  // A and B, five planes each (80 KB)
-constexpr int kHalf = BN / 2;                          // epilogue: 64 columns at a time
-constexpr int LDR = kHalf + 2;                         // row-major staging, in float2 (h, l)
-constexpr int LDC = BM + 2;                            // column-major staging, in float2
-constexpr int kEpiBytes = (BM * LDR > kHalf * LDC ? BM * LDR : kHalf * LDC) * 8;
+constexpr int kThreads = 256;                          // eight warps
+constexpr int kChunk = 16;                             // epilogue: columns per tcgen05.ld
 __host__ __device__ constexpr int cmax(int a, int b) { return a > b ? a : b; }
 // variant 0: two stages; variant 1: one stage.  The four accumulators hold all 512
 // tensor-memory columns, so the shared memory asked for is at least kOneCtaBytes,
@@ -66,7 +68,7 @@ __host__ __device__ constexpr int cmax(int a, int b) { return a > b ? a : b; }
 constexpr int kStages0 = 2, kStages1 = 1;
 constexpr int kOneCtaBytes = 120 * 1024;
 constexpr int smem_bytes(int stages) {
-    return cmax(cmax(stages * kStageBytes, kEpiBytes) + 1024 + 128, kOneCtaBytes);
+    return cmax(stages * kStageBytes + 1024 + 128, kOneCtaBytes);
 }
 constexpr int kAccs = 4;
 constexpr uint32_t kTmemCols = kAccs * BN;   // 512: acc0 .. acc3
@@ -160,21 +162,27 @@ __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
     e = (a - (s - bp)) + (b - bp);
 }
 
-// the five digit planes of q = qh + ql (an unevaluated pair): d_a = rint of the
-// remainder times 2^7a, stored as d_a 2^-7a; each subtraction of a digit is exact
-__device__ __forceinline__ void planes(float qh, float ql, __nv_bfloat16 *o) {
-    float rh, rl;
-    two_sum(qh, ql, rh, rl);
-    float w = 1.0f;
+// the five digits of q = qh + ql (|q| <= 64, |ql| <= ulp(qh) / 2), each times its
+// weight 2^-7a: d_a = rint of the remainder scaled by 2^7a.  r - rint(r) and the
+// scaling by 2^7 are exact, so d0, d1, d2 are exact digits of qh (|d| <= 64); ql
+// (at most 2^-18 when |qh| < 64) joins the remainder after them, which rounds
+// once at ~2^-39 of q, and d3 may reach 68 (its pairs are summed in FP32 in any
+// case).  The five digits leave q - sum d_a 2^-7a within 2^-29.
+__device__ __forceinline__ void digits(float qh, float ql, float *o) {
+    float r = qh;
 #pragma unroll
     for (int a = 0; a < kPieces; ++a) {
-        const float d = rintf(rh);
-        o[a] = __float2bfloat16_rn(d * w);  // a 7-bit integer times a power of two: exact
-        two_sum(rh - d, rl, rh, rl);
-        rh *= 128.0f;
-        rl *= 128.0f;
-        w *= 1.0f / 128.0f;
+        const float d = rintf(r);
+        o[a] = d * __int_as_float((127 - 7 * a) << 23);  // d 2^-7a: exact
+        r = a == 2 ? fmaf(ql, 2097152.0f, (r - d) * 128.0f) : (r - d) * 128.0f;
     }
+}
+// the same as BF16 planes (d 2^-7a has at most 7 significant bits: exact in BF16)
+__device__ __forceinline__ void planes(float qh, float ql, __nv_bfloat16 *o) {
+    float v[kPieces];
+    digits(qh, ql, v);
+#pragma unroll
+    for (int a = 0; a < kPieces; ++a) o[a] = __float2bfloat16_rn(v[a]);
 }
 
 // coef (acc0 + acc1 + acc2 + acc3) + d as an unevaluated float pair (h, l): the
@@ -201,17 +209,37 @@ struct Maps {
     CUtensorMap a[kPieces], b[kPieces];
 };
 
+// a bounded wait that also ends when *abort is set (by the CTA's other role)
+__device__ __forceinline__ bool mbar_wait_or(uint64_t *bar, uint32_t parity, long long limit, volatile int *abort) {
+    for (long long it = 0; it < limit; ++it) {
+        uint32_t done;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(smem_u32(bar)), "r"(parity)
+            : "memory");
+        if (done) return true;
+        if (*abort) return false;
+    }
+    return false;
+}
+
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
+    __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<uint32_t *>(&v);
+}
+
 template <int kStages>
-__global__ void __launch_bounds__(128, 1)
+__global__ void __launch_bounds__(kThreads, 1)
     k_tc_gemm(const __grid_constant__ Maps maps, TcOut out, int npad, const int *live, const int *nlist, float alpha,
               float diag, float in_scale, int sym, long long spin_limit, int issue_loads) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    uint64_t *full = (uint64_t *)(smem + cmax(kStages * kStageBytes, kEpiBytes));
+    uint64_t *full = (uint64_t *)(smem + kStages * kStageBytes);
     uint64_t *empty = full + kStages;
     uint64_t *done = empty + kStages;
     uint32_t *tmem_slot = (uint32_t *)(done + 1);
-    __shared__ int s_fail;
+    __shared__ int s_fail, s_issued, s_landed;
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int tiles_n = npad / BN;
@@ -232,6 +260,8 @@ __global__ void __launch_bounds__(128, 1)
         }
         mbar_init(done, 1);
         s_fail = 0;
+        s_issued = 0;
+        s_landed = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0) {
@@ -243,13 +273,19 @@ __global__ void __launch_bounds__(128, 1)
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = *tmem_slot;
+    volatile int *fail = &s_fail;
 
-    if (tid == 0) {
-        const uint32_t idesc = instr_desc(BM, BN);
-        int issued = 0, landed = 0;  // chunks whose loads were issued / have been waited for
-        auto load = [&](int kc) {
-            if (!issue_loads) return;  // the expiry test: nothing is issued, nothing is in flight
+    if (warp == 1 && lane == 0) {
+        // TMA producer: chunk kc goes to stage kc mod kStages once the MMAs of chunk
+        // kc - kStages have released it (the expiry test issues nothing)
+        int issued = 0;
+        for (int kc = 0; kc < nk && issue_loads; ++kc) {
             const int s = kc % kStages;
+            if (kc >= kStages && !mbar_wait_or(&empty[s], (uint32_t)(kc / kStages - 1) & 1u, spin_limit, fail)) {
+                *fail = 1;
+                break;
+            }
+            if (*fail) break;
             unsigned char *st = smem + s * kStageBytes;
             mbar_expect_tx(&full[s], kStageBytes);
             for (int p = 0; p < kPieces; ++p) {
@@ -257,14 +293,19 @@ __global__ void __launch_bounds__(128, 1)
                 tma_load_3d(st + (kPieces + p) * kTileBytes, &maps.b[p], kc * BK, n0, slot, &full[s]);
             }
             ++issued;
-        };
-        bool ok = true;
-        for (int kc = 0; kc < kStages && kc < nk; ++kc) load(kc);
-        for (int kc = 0; kc < nk && ok; ++kc) {
+        }
+        s_issued = issued;
+    } else if (warp == 0 && lane == 0) {
+        // MMA issuer: the nineteen plane products of each landed chunk, then its stage
+        // is released by a commit
+        const uint32_t idesc = instr_desc(BM, BN);
+        int landed = 0;
+        for (int kc = 0; kc < nk; ++kc) {
             const int s = kc % kStages;
-            const uint32_t use = (uint32_t)(kc / kStages) & 1u;
-            ok = mbar_wait(&full[s], use, spin_limit);
-            if (!ok) break;
+            if (!mbar_wait_or(&full[s], (uint32_t)(kc / kStages) & 1u, spin_limit, fail)) {
+                *fail = 1;
+                break;
+            }
             ++landed;
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             const uint32_t base = smem_u32(smem + s * kStageBytes);
@@ -280,20 +321,8 @@ __global__ void __launch_bounds__(128, 1)
                     mma_bf16(tmem + (uint32_t)(ac * BN), ad, bd, idesc, acc);
                 }
             mma_commit(&empty[s]);
-            // refill this stage once its MMAs have read it
-            if (kc + kStages < nk) {
-                ok = mbar_wait(&empty[s], use, spin_limit);
-                if (!ok) break;
-                load(kc + kStages);
-            }
         }
-        if (!ok) {
-            s_fail = 1;
-            // loads still in flight write this CTA's shared memory: give them their
-            // own bounded wait before the block can exit and the memory is reused
-            for (int j = landed; j < issued; ++j)
-                mbar_wait(&full[j % kStages], (uint32_t)(j / kStages) & 1u, kSpinLimit);
-        }
+        s_landed = landed;
         mma_commit(done);
     }
     __syncwarp();
@@ -302,110 +331,106 @@ __global__ void __launch_bounds__(128, 1)
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const int bad = __syncthreads_or(!ok || s_fail);
     if (bad) {
-        if (tid == 0 && out.err) atomicExch(out.err, MCB_ERR_ITER);
+        if (tid == 0) {
+            if (out.err) atomicExch(out.err, MCB_ERR_ITER);
+            // loads still in flight write this CTA's shared memory: give them their
+            // own bounded wait before the block can exit and the memory is reused
+            for (int j = s_landed; j < s_issued; ++j)
+                mbar_wait(&full[j % kStages], (uint32_t)(j / kStages) & 1u, kSpinLimit);
+        }
     } else {
         const int n = nlist[blockIdx.y];
         const float coef = alpha * in_scale;
         const double fscale = out.slot_scale ? out.slot_scale[slot] : 1.0;
-        // Stores go through shared-memory tiles (the stage buffers are free once the
-        // MMAs are done), 64 columns of the tile at a time, so that every global
-        // store is coalesced.  Symmetric products: the lower triangle is stored
-        // twice, as (row, col) from a row-major tile and mirrored to (col, row)
-        // from a column-major one (the accumulators are read a second time for it),
-        // so the result is exactly symmetric; diagonal tiles store their lower part.
-        float2 *F = (float2 *)smem;
-        const int r = warp * 32 + lane;
+        const int g = warp & 3;         // tensor-memory lanes 32 g .. 32 g + 31: tile rows
+        const int r = g * 32 + lane;    // this thread's tile row
+        const int row = m0 + r;
         const bool diag_tile = sym && ti == tj;
         const size_t sb = (size_t)slot * out.stride;
-        auto dval = [&](int row, int col) { return (row == col && row < n) ? diag : 0.0f; };
-        // store elements valid_from .. valid_to of four consecutive values
-        auto store4 = [&](size_t o, const float2 *x, int valid_from, int valid_to) {
-            __nv_bfloat16 pl[4][kPieces];
-#pragma unroll
-            for (int e = 0; e < 4; ++e) planes(x[e].x * out.pscale, x[e].y * out.pscale, pl[e]);
-            if (valid_from == 0 && valid_to == 3) {
-                if (out.f32)
-                    *reinterpret_cast<float4 *>(out.f32 + o) =
-                        make_float4(x[0].x + x[0].y, x[1].x + x[1].y, x[2].x + x[2].y, x[3].x + x[3].y);
-                if (out.f64) {
-                    reinterpret_cast<double2 *>(out.f64 + o)[0] = make_double2(
-                        fscale * ((double)x[0].x + (double)x[0].y), fscale * ((double)x[1].x + (double)x[1].y));
-                    reinterpret_cast<double2 *>(out.f64 + o)[1] = make_double2(
-                        fscale * ((double)x[2].x + (double)x[2].y), fscale * ((double)x[3].x + (double)x[3].y));
-                }
-                if (out.p[0]) {
-#pragma unroll
-                    for (int p = 0; p < kPieces; ++p) {
-                        __nv_bfloat162 a = __halves2bfloat162(pl[0][p], pl[1][p]);
-                        __nv_bfloat162 b = __halves2bfloat162(pl[2][p], pl[3][p]);
-                        *reinterpret_cast<uint2 *>(out.p[p] + o) =
-                            make_uint2(*reinterpret_cast<uint32_t *>(&a), *reinterpret_cast<uint32_t *>(&b));
-                    }
-                }
-            } else {
-#pragma unroll
-                for (int e = 0; e < 4; ++e) {
-                    if (e < valid_from || e > valid_to) continue;
-                    if (out.f32) out.f32[o + e] = x[e].x + x[e].y;
-                    if (out.f64) out.f64[o + e] = fscale * ((double)x[e].x + (double)x[e].y);
-                    if (out.p[0])
-#pragma unroll
-                        for (int p = 0; p < kPieces; ++p) out.p[p][o + e] = pl[e][p];
-                }
-            }
-        };
-        for (int half = 0; half < 2; ++half) {
-            const int cb = half * kHalf;
-            // (1) row-major tile F[r][c] = C(m0 + r, n0 + cb + c), c < 64
-            for (int c0 = 0; c0 < kHalf; c0 += 16) {
-                float v[kAccs][16];
+        const bool want_planes = out.p[0] != nullptr;
+        for (int c0 = (warp >> 2) * (BN / 2); c0 < (warp >> 2) * (BN / 2) + BN / 2; c0 += kChunk) {
+            float h[kChunk], l[kChunk];
+            {
+                float v[kAccs][kChunk];
 #pragma unroll
                 for (int a = 0; a < kAccs; ++a)
-                    tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(a * BN + cb + c0), v[a]);
+                    tmem_ld16(tmem + ((uint32_t)(g * 32) << 16) + (uint32_t)(a * BN + c0), v[a]);
 #pragma unroll
-                for (int j = 0; j < 16; ++j)
-                    F[r * LDR + c0 + j] =
-                        ff_value(v[0][j], v[1][j], v[2][j], v[3][j], coef, dval(m0 + r, n0 + cb + c0 + j));
-            }
-            __syncthreads();
-            // direct half: a half-warp per row, four columns per lane; diagonal tiles
-            // keep col <= row
-            for (int rr = warp * 2 + (lane >> 4); rr < BM; rr += 8) {
-                const int c = 4 * (lane & 15);
-                const int col = cb + c;
-                if (diag_tile && col > rr) continue;
-                float2 x[4];
-#pragma unroll
-                for (int e = 0; e < 4; ++e) x[e] = F[rr * LDR + c + e];
-                store4(sb + (size_t)(m0 + rr) * npad + n0 + col, x, 0, diag_tile ? min(3, rr - col) : 3);
-            }
-            __syncthreads();
-            if (sym) {
-                // (2) column-major tile F[c][r] = C(m0 + r, n0 + cb + c), from the accumulators again
-                for (int c0 = 0; c0 < kHalf; c0 += 16) {
-                    float v[kAccs][16];
-#pragma unroll
-                    for (int a = 0; a < kAccs; ++a)
-                        tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(a * BN + cb + c0), v[a]);
-#pragma unroll
-                    for (int j = 0; j < 16; ++j)
-                        F[(c0 + j) * LDC + r] =
-                            ff_value(v[0][j], v[1][j], v[2][j], v[3][j], coef, dval(m0 + r, n0 + cb + c0 + j));
+                for (int j = 0; j < kChunk; ++j) {
+                    const int col = n0 + c0 + j;
+                    const float2 x =
+                        ff_value(v[0][j], v[1][j], v[2][j], v[3][j], coef, (row == col && row < n) ? diag : 0.0f);
+                    h[j] = x.x;
+                    l[j] = x.y;
                 }
-                __syncthreads();
-                // mirrored half: output row n0 + cb + cc, a lane per four rows of the
-                // tile; diagonal tiles keep rows strictly below the diagonal (rr > col)
-                for (int cc = warp; cc < kHalf; cc += 4) {
-                    const int rr0 = 4 * lane;
-                    const int col = cb + cc;
-                    const int from = diag_tile ? max(0, col + 1 - rr0) : 0;
-                    if (from >= 4) continue;
-                    float2 x[4];
+            }
+            // the element's digit planes, packed in pairs of consecutive columns
+            uint32_t pk[kPieces][kChunk / 2];
+            if (want_planes) {
 #pragma unroll
-                    for (int e = 0; e < 4; ++e) x[e] = F[cc * LDC + rr0 + e];
-                    store4(sb + (size_t)(n0 + col) * npad + m0 + rr0, x, from, 3);
+                for (int j = 0; j < kChunk; j += 2) {
+                    float d0[kPieces], d1[kPieces];
+                    digits(h[j] * out.pscale, l[j] * out.pscale, d0);
+                    digits(h[j + 1] * out.pscale, l[j + 1] * out.pscale, d1);
+#pragma unroll
+                    for (int p = 0; p < kPieces; ++p) pk[p][j / 2] = pack_bf16(d0[p], d1[p]);
                 }
-                __syncthreads();
+            }
+            // this row's 16 columns; a diagonal tile stores its own lower triangle
+            // (col <= row) element by element, and every element of a symmetric
+            // product goes to its mirror too (col < row on a diagonal tile); lanes are
+            // consecutive rows, so a mirror store is consecutive across the warp
+            const size_t od = sb + (size_t)row * npad + n0 + c0;
+            const size_t om = sb + (size_t)(n0 + c0) * npad + row;  // mirror of column c0
+            auto own = [&](int j) { return diag_tile && c0 + j <= r; };
+            auto mirror = [&](int j) { return sym && (!diag_tile || c0 + j < r); };
+            if (out.f32) {
+                float f[kChunk];
+#pragma unroll
+                for (int j = 0; j < kChunk; ++j) f[j] = h[j] + l[j];
+                if (!diag_tile) {
+                    float4 *o4 = reinterpret_cast<float4 *>(out.f32 + od);
+#pragma unroll
+                    for (int q = 0; q < kChunk / 4; ++q) o4[q] = make_float4(f[4 * q], f[4 * q + 1], f[4 * q + 2], f[4 * q + 3]);
+                }
+#pragma unroll
+                for (int j = 0; j < kChunk; ++j) {
+                    if (own(j)) out.f32[od + j] = f[j];
+                    if (mirror(j)) out.f32[om + (size_t)j * npad] = f[j];
+                }
+            }
+            if (out.f64) {
+                double dv[kChunk];
+#pragma unroll
+                for (int j = 0; j < kChunk; ++j) dv[j] = fscale * ((double)h[j] + (double)l[j]);
+                if (!diag_tile) {
+                    double2 *o2 = reinterpret_cast<double2 *>(out.f64 + od);
+#pragma unroll
+                    for (int q = 0; q < kChunk / 2; ++q) o2[q] = make_double2(dv[2 * q], dv[2 * q + 1]);
+                }
+#pragma unroll
+                for (int j = 0; j < kChunk; ++j) {
+                    if (own(j)) out.f64[od + j] = dv[j];
+                    if (mirror(j)) out.f64[om + (size_t)j * npad] = dv[j];
+                }
+            }
+            if (want_planes) {
+#pragma unroll
+                for (int p = 0; p < kPieces; ++p) {
+                    __nv_bfloat16 *o = out.p[p];
+                    if (!diag_tile) {
+                        uint4 *o4 = reinterpret_cast<uint4 *>(o + od);
+                        o4[0] = make_uint4(pk[p][0], pk[p][1], pk[p][2], pk[p][3]);
+                        o4[1] = make_uint4(pk[p][4], pk[p][5], pk[p][6], pk[p][7]);
+                    }
+#pragma unroll
+                    for (int j = 0; j < kChunk; ++j) {
+                        const uint32_t w = pk[p][j / 2];
+                        const __nv_bfloat16 b = __ushort_as_bfloat16((unsigned short)((j & 1) ? (w >> 16) : (w & 0xffffu)));
+                        if (own(j)) o[od + j] = b;
+                        if (mirror(j)) o[om + (size_t)j * npad] = b;
+                    }
+                }
             }
         }
     }
@@ -508,10 +533,10 @@ int tc_gemm(const void *amaps, const void *bmaps, const TcOut &out, int npad, in
     const int test = g_test_expiry.load();
     const long long spins = test ? kTestSpinLimit : kSpinLimit;
     if (variant == 0)
-        k_tc_gemm<kStages0><<<grid, 128, smem_bytes(kStages0), st>>>(m, out, npad, d_live, d_n, alpha, diag, in_scale,
+        k_tc_gemm<kStages0><<<grid, kThreads, smem_bytes(kStages0), st>>>(m, out, npad, d_live, d_n, alpha, diag, in_scale,
                                                                      sym, spins, !test);
     else
-        k_tc_gemm<kStages1><<<grid, 128, smem_bytes(kStages1), st>>>(m, out, npad, d_live, d_n, alpha, diag, in_scale,
+        k_tc_gemm<kStages1><<<grid, kThreads, smem_bytes(kStages1), st>>>(m, out, npad, d_live, d_n, alpha, diag, in_scale,
                                                                      sym, spins, !test);
     return cudaGetLastError() == cudaSuccess ? MCB_OK : MCB_ERR_CUDA;
 }

@@ -2,9 +2,10 @@
 //
 // Operand format.  A matrix x with a power-of-two scale sigma (|x| <= sigma / 2
 // for the exactness bounds below) is carried as q = x 2^7 / sigma cut into five
-// signed 7-bit digits, q = d0 + d1 2^-7 + d2 2^-14 + d3 2^-21 + d4 2^-28 (each
-// |d_a| <= 64, rounded to nearest, 35 bits in all), digit a stored as the BF16
-// value d_a 2^-7a (exact): five BF16 planes per matrix.  A product of two such
+// signed digits, q = d0 + d1 2^-7 + d2 2^-14 + d3 2^-21 + d4 2^-28 (each rounded
+// to nearest, |d_a| <= 64; d3 may reach 68 where a float pair is cut, and only
+// enters the FP32 group below), digit a stored as the BF16 value d_a 2^-7a
+// (exact): five BF16 planes per matrix, q to within 2^-29.  A product of two such
 // matrices is a sum over digit pairs; the pairs of digit sum 0, 1 and 2 give
 // integer multiples of 2^0, 2^-7, 2^-14 below 2^24 in magnitude (for K <= 1024),
 // which FP32 accumulators hold exactly, and the pairs of digit sum 3 to 5 are

@@ -1,12 +1,13 @@
 """The chosen form: Newton-Schulz PSD projection on the tensor cores.
 
 Checks (1) the projection against an FP64 eigendecomposition (numpy.linalg.eigh)
-for FP32-accurate operands (default) and for one-pass operands, whose rounding
-floor is stated; (2) node bounds against the CPU oracle's FP64 method: the
-bound is the same safe dual bound n lambda_max(L - Diag y - B^T s) + sum y +
-sum s, so it stays valid whatever the projection's error, and it agrees with the
-FP64 method to the ADMM's own stopping tolerance (minTol = 1e-3); (3) whole
-branch-and-bound runs reach the reference's optimum and optimal cut.
+for the default digit-plane operands (five BF16 digits, products accurate to
+~5e-10) and for one-pass operands, whose rounding floor is stated; (2) node
+bounds against the CPU oracle's FP64 method: the bound is the same safe dual
+bound n lambda_max(L - Diag y - B^T s) + sum y + sum s, so it stays valid
+whatever the projection's error, and it agrees with the FP64 method to 1e-6
+relative, after the same number of ADMM iterations; (3) whole branch-and-bound
+runs reach the reference's optimum and optimal cut.
 """
 import json
 import os
@@ -48,13 +49,14 @@ def test_ns_projection_against_eigh(gpu_lib, n, form):
         Xr, Mr = _proj_eigh(W)
         Xp, Q, Z, _ = M.project(W, proj)
         err = np.linalg.norm(Xp - Xr) / np.linalg.norm(W)
-        # FP32-accurate operands: the error is the FP32 rounding of the iteration
-        assert err < 5e-6, (name, err)
+        # digit-plane operands: ~5e-9 of ||W|| at n = 512 (the sign iteration's own
+        # resolution of the eigenvalues nearest 0)
+        assert err < 3e-8, (name, err)
         assert np.array_equal(Xp, Xp.T)
         assert np.allclose(np.tril(Q), np.tril(Xp - W), atol=1e-12)
         if name == "admm":  # a spectral gap around 0: the count is exact
             assert Z.shape[1] == Mr
-            assert np.isclose(np.trace(Xp), np.trace(Xr), rtol=1e-5)
+            assert np.isclose(np.trace(Xp), np.trace(Xr), rtol=1e-7)
 
 
 def test_ns_one_pass_operands_have_a_rounding_floor(gpu_lib):
@@ -116,10 +118,10 @@ def test_ns_node_bound_against_oracle(gpu_lib, orc, n, p, wts, seed, fixed, pent
     for proj in (M.PROJ_NS_BF16, M.PROJ_NS_TF32):
         ctx = M.Context(M.params(include_Pent=pent, include_Hepta=0, use_diff=0), SL, nv, flags=proj)
         bg, sg = ctx.evaluate(M.node(fixed), rank=1)
-        assert abs(bg - bo) <= 2e-3 * abs(bo), (bg, bo)
+        assert abs(bg - bo) <= 1e-6 * abs(bo), (bg, bo)
         # the node's best cut (found by either heuristic) never exceeds a safe bound
         assert bg >= max(ctx.lb()[0], oc.lb()[0])
-        assert abs(sg.admm_iters - so.admm_iters) <= 0.25 * so.admm_iters + 20
+        assert sg.admm_iters == so.admm_iters and sg.outer_iters == so.outer_iters
         ctx.close()
 
 
@@ -144,14 +146,15 @@ def test_ns_branch_and_bound_reaches_reference_optimum(gpu_lib, fx):
 
 @pytest.mark.parametrize("npad,batch", [(128, 1), (256, 3), (512, 2)])
 def test_tcgen05_split_gemm_against_float64(gpu_lib, npad, batch):
-    """The tensor-core GEMM with three-piece BF16 operands is FP32-accurate on
-    general (non-symmetric) matrices: C = alpha A B^T + diag I."""
+    """The tensor-core GEMM with digit-plane operands on general (non-symmetric)
+    matrices, C = alpha A B^T + diag I: its FP32 output is the rounding of a
+    product accurate to ~5e-10, so the error is FP32's half ulp of the largest entry."""
     rng = np.random.default_rng(npad + batch)
     A = rng.standard_normal((batch, npad, npad)).astype(np.float32)
     B = rng.standard_normal((batch, npad, npad)).astype(np.float32)
     C = gpu_lib.split_gemm(A, B, alpha=-0.75, diag=1.5)
     ref = -0.75 * np.einsum("bik,bjk->bij", A.astype(np.float64), B.astype(np.float64)) + 1.5 * np.eye(npad)
-    assert np.abs(C - ref).max() <= 1e-5 * np.abs(ref).max()
+    assert np.abs(C - ref).max() <= 1e-7 * np.abs(ref).max()
 
 
 def test_tcgen05_split_gemm_rejects_bad_sizes(gpu_lib):
@@ -162,14 +165,14 @@ def test_tcgen05_split_gemm_rejects_bad_sizes(gpu_lib):
 @pytest.mark.parametrize("npad", [128, 384])
 def test_tcgen05_symmetric_product_is_exactly_symmetric(gpu_lib, npad):
     """sym = 1: lower tiles computed and mirrored; the result is bit-symmetric and
-    FP32-accurate for a product known to be symmetric (A A^T)."""
+    FP32-exact (to the output's rounding) for a product known to be symmetric (A A^T)."""
     rng = np.random.default_rng(npad)
     A = rng.standard_normal((2, npad, npad)).astype(np.float32)
     A = A + A.transpose(0, 2, 1)
     C = gpu_lib.split_gemm(A, A, alpha=0.5, diag=-1.0, sym=True)
     ref = 0.5 * np.einsum("bik,bjk->bij", A.astype(np.float64), A.astype(np.float64)) - np.eye(npad)
     assert np.array_equal(C, C.transpose(0, 2, 1))
-    assert np.abs(C - ref).max() <= 1e-5 * np.abs(ref).max()
+    assert np.abs(C - ref).max() <= 1e-7 * np.abs(ref).max()
 
 
 @pytest.mark.parametrize("proj", ["fp64", "ns"])
