@@ -458,8 +458,8 @@ int launch_admm_iteration(mcb_ctx *c, int ns, int mmax, int emax) {
     { Prof p(c, K_RHS, 1); launch_admm_rhs(d, ns, N, mmax, c->st); }
     {
         // the plain form solves to 1e-13 (the reference's direct factorisation agrees
-        // to rounding); the Newton-Schulz forms carry 1e-7 projection errors, so a
-        // 1e-10 solve is still far below anything the ADMM's 1e-3 tolerance sees
+        // to rounding); the Newton-Schulz forms carry projection errors of ~5e-9 of
+        // ||W||, so a 1e-10 solve stays below them
         Prof p(c, K_CG, 1);
         launch_cg(d, ns, c->cg_max_iters, c->proj == MCB_PROJ_FP64 ? 1e-13 : 1e-10, c->st);
     }
