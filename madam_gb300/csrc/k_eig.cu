@@ -101,39 +101,49 @@ __global__ void __launch_bounds__(512) k_tridiag(Slot *slots, int gate) {
 // ---------------------------------------------------------------------------
 // The same reduction with a slot's rows spread over the C CTAs of a thread-block
 // cluster (C = gridDim.x), so that a node's 4/3 n^3 FP64 flops run on C SMs'
-// FP64 pipes.  At step k the trailing rows k+1+i, i in [0, m), are dealt in chunks
-// of ceil(m / C): CTA c owns chunk c (CTA 0 always owns i = 0) and reads and writes
-// only its own rows of A, so the symmetric product w = tau A22 v and the rank-2
-// update need no exchange of matrix data.  The exchanges go through the slot's
-// work array s.dwork (w, and per-CTA partial sums added in CTA order, so every CTA
-// gets the same sigma^2 and v^T w), with two cluster barriers per step (release /
-// acquire at cluster scope): after the sigma^2 partials (which also publishes the
-// previous step's update of column k) and after w.  Every CTA of a cluster runs
-// the same loop with the same barrier sequence (the slot, n and tau are common to
-// the cluster), so the barriers always match.
+// FP64 pipes.  Rows are owned statically, in blocks of 32: block b (rows 32 b ..
+// 32 b + 31) belongs to CTA b mod C for the whole reduction, which reads and
+// writes only its own rows of A, so the product w = tau A22 v and the rank-2
+// update need no exchange of matrix data, and the column-k entries a CTA sums for
+// sigma^2 at step k are ones it updated itself at step k - 1.  The exchanges go
+// through the slot's work array s.dwork (w, and per-CTA partial sums added in CTA
+// order, so every CTA gets the same sigma^2 and v^T w), with two cluster barriers
+// per step (release / acquire at cluster scope): after the sigma^2 partials
+// (which also publishes the previous step's update to every CTA before any of
+// them reads column k or the rows of another CTA) and after w.  Every CTA of a
+// cluster runs the same loop with the same barrier sequence (the slot, n and tau
+// are common to the cluster), so the barriers always match.  Within a CTA the
+// warps split the columns of A22 v and of the update, and the lanes take 32
+// consecutive rows of an own block (coalesced column reads).
+constexpr int kTrMaxBlk = 4;  // own row blocks per CTA: ceil(ceil(n / 32) / C) <= 4 for n <= 1024
 __global__ void __launch_bounds__(512) k_tridiag_cl(Slot *slots, int gate) {
     Slot &s = slots[blockIdx.y];
     if (!gated(s, gate)) return;  // common to the cluster: the CTAs of one slot
     namespace cg = cooperative_groups;
     cg::cluster_group cl = cg::this_cluster();
-    const int n = s.n, tid = threadIdx.x, bs = blockDim.x;
+    const int n = s.n, tid = threadIdx.x, bs = blockDim.x, lane = tid & 31, wid = tid >> 5, nw = bs >> 5;
     const int C = gridDim.x, c = blockIdx.x;
+    const int nblk = (n + 31) >> 5;
+    const int myblk = (nblk - c + C - 1) / C;  // blocks c, c + C, c + 2C, ...
     double *A = s.A;
     extern __shared__ double sh[];
-    double *v = sh, *w = sh + n, *red = sh + 2 * n;
+    double *v = sh, *w = sh + n, *red = sh + 2 * n, *part = red + 40;  // part: nw x 32 kTrMaxBlk
     double *gw = s.dwork, *gp = s.dwork + n;  // w; partials: [0, C) sigma^2, [C, 2C) v^T w
+    auto own_row = [&](int q) { return (c + q * C) * 32 + lane; };
     for (int k = 0; k < n - 2; ++k) {
-        const int m = n - k - 1;
-        const int chunk = (m + C - 1) / C, i0 = min(m, c * chunk), i1 = min(m, i0 + chunk);
-        double *x = A + (k + 1) + (size_t)k * n;
+        const int m = n - k - 1, r0 = k + 1;  // trailing rows / columns r0 .. n-1, local i = r - r0
+        const double *colk = A + (size_t)k * n;
         double loc = 0.0;
-        for (int i = max(i0, 1) + tid; i < i1; i += bs) loc += x[i] * x[i];
+        for (int q = wid; q < myblk; q += nw) {
+            const int r = own_row(q);
+            if (r >= k + 2 && r < n) loc += colk[r] * colk[r];
+        }
         loc = block_sum(loc, red);
         if (tid == 0) gp[c] = loc;
         cl.sync();
         double sig2 = 0.0;
         for (int q = 0; q < C; ++q) sig2 += gp[q];
-        const double alpha = x[0];
+        const double alpha = colk[r0];
         double beta, tau, scal;
         if (sig2 == 0.0) {
             beta = alpha;
@@ -144,24 +154,44 @@ __global__ void __launch_bounds__(512) k_tridiag_cl(Slot *slots, int gate) {
             tau = (beta - alpha) / beta;
             scal = 1.0 / (alpha - beta);
         }
-        for (int i = tid; i < m; i += bs) v[i] = i == 0 ? 1.0 : x[i] * scal;
+        for (int i = tid; i < m; i += bs) v[i] = i == 0 ? 1.0 : colk[r0 + i] * scal;
         __syncthreads();
         if (tau != 0.0) {
-            const double *A22 = A + (k + 1) + (size_t)(k + 1) * n;
+            double acc[kTrMaxBlk];
+#pragma unroll
+            for (int q = 0; q < kTrMaxBlk; ++q) acc[q] = 0.0;
+            for (int j = wid; j < m; j += nw) {
+                const double vj = v[j];
+                const double *col = A + (size_t)(r0 + j) * n;
+#pragma unroll
+                for (int q = 0; q < kTrMaxBlk; ++q) {
+                    const int r = own_row(q);
+                    if (q < myblk && r >= r0 && r < n) acc[q] += col[r] * vj;
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < kTrMaxBlk; ++q) part[(wid * kTrMaxBlk + q) * 32 + lane] = acc[q];
+            __syncthreads();
             double lp = 0.0;
-            for (int i = i0 + tid; i < i1; i += bs) {
-                double acc = 0.0;
-                for (int j = 0; j < m; ++j) acc += A22[i + (size_t)j * n] * v[j];
-                const double wi = tau * acc;
-                gw[i] = wi;
-                lp += wi * v[i];
+            for (int t = tid; t < myblk * 32; t += bs) {
+                const int q = t >> 5, r = (c + q * C) * 32 + (t & 31);
+                if (r >= r0 && r < n) {
+                    double a = 0.0;
+                    for (int u = 0; u < nw; ++u) a += part[(u * kTrMaxBlk + q) * 32 + (t & 31)];
+                    const double wi = tau * a;
+                    gw[r - r0] = wi;
+                    lp += wi * v[r - r0];
+                }
             }
             lp = block_sum(lp, red);
             if (tid == 0) gp[C + c] = lp;
         }
         cl.sync();
         // every CTA has read column k: store the reflector in its own rows
-        for (int i = max(i0, 1) + tid; i < i1; i += bs) x[i] = v[i];
+        for (int q = wid; q < myblk; q += nw) {
+            const int r = own_row(q);
+            if (r >= k + 2 && r < n) A[r + (size_t)k * n] = v[r - r0];
+        }
         if (c == 0 && tid == 0) {
             s.d[k] = A[k + (size_t)k * n];
             s.e[k] = beta;
@@ -173,11 +203,14 @@ __global__ void __launch_bounds__(512) k_tridiag_cl(Slot *slots, int gate) {
             const double K = -0.5 * tau * pv;
             for (int i = tid; i < m; i += bs) w[i] = gw[i] + K * v[i];
             __syncthreads();
-            double *U = A + (k + 1) + (size_t)(k + 1) * n;
-            const int rows = i1 - i0;
-            for (int idx = tid; idx < rows * m; idx += bs) {
-                const int j = idx / rows, i = i0 + idx - j * rows;
-                U[i + (size_t)j * n] -= v[i] * w[j] + w[i] * v[j];
+            for (int j = wid; j < m; j += nw) {
+                const double vj = v[j], wj = w[j];
+                double *col = A + (size_t)(r0 + j) * n;
+#pragma unroll
+                for (int q = 0; q < kTrMaxBlk; ++q) {
+                    const int r = own_row(q);
+                    if (q < myblk && r >= r0 && r < n) col[r] -= v[r - r0] * wj + w[r - r0] * vj;
+                }
             }
         }
         __syncthreads();
@@ -653,6 +686,12 @@ void launch_tridiag(Slot *d_slots, int nslots, int nmax, int gate, cudaStream_t 
         k_tridiag<<<nslots, 512, sm, st>>>(d_slots, gate);
         return;
     }
+    // the cluster kernel's own row blocks: at most kTrMaxBlk per CTA (n <= 1024)
+    if (((nmax + 31) / 32 + C - 1) / C > kTrMaxBlk) {
+        k_tridiag<<<nslots, 512, sm, st>>>(d_slots, gate);
+        return;
+    }
+    sm += (size_t)(512 / 32) * kTrMaxBlk * 32 * sizeof(double);
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(C, nslots);
     cfg.blockDim = dim3(512);
