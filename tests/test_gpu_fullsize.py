@@ -81,7 +81,12 @@ def test_fullsize_node_bounds_match_oracle(gpu_lib, name, form):
                 abs(sg.basic_bound - r["basic_bound"]) > 1e-9 * abs(r["basic_bound"]):
             bad.append((r["node"], bg, r["bound"], got, want))
     assert not bad, bad
-    assert ctx_lb == INCUMBENT[name]
+    if form == "fp64":
+        assert ctx_lb == INCUMBENT[name]
+    else:
+        # the chosen form's own rounding heuristic (hyperplanes through X v, 1-opt on
+        # the GPU) may find a better cut than the oracle's; never a worse incumbent
+        assert ctx_lb >= INCUMBENT[name]
 
 
 @pytest.mark.parametrize("fx", PUBLISHED, ids=lambda f: f["name"].replace("/", "_"))
