@@ -17,8 +17,10 @@ timed on the host; `plain_fp64` is the plain form on the same workload in the
 same run, and `time_to_optimum` a full branch-and-bound of a seeded G(100, 0.5)
 unit-weight instance (triangle cuts) in both forms.  `n512` compares the forms on
 G(512, 0.1) with integer weights in [-10, 10] (node throughput, bound agreement,
-and a time-capped branch-and-bound of the whole graph); `uneven_batch` bounds the
-roots of 2000 seeded independent subproblems of uneven order in one call.  Both
+and a time-capped branch-and-bound of the whole graph); `torus` bounds nodes of
+the 20 x 20 toroidal spin glass (n = 400, all three families) against the
+oracle's stored answers; `uneven_batch` bounds the roots of 2000 seeded
+independent subproblems of uneven order in one call.  Both
 arms print the same `config` (the workload); the reference arm (`--impl
 reference`) runs the reference's method on the host cores, one process per core
 started before the timed steps.
@@ -195,7 +197,8 @@ FORMS = {"learned": "Newton-Schulz projection (BF16 split operands, FP64 product
 TTO = dict(n=100, p=0.5, weights="one", seed=1101, params=dict(include_Pent=0, include_Hepta=0))
 
 
-DTYPES = {"learned": "bf16 split (FP32-accurate) + f64", "mixed": "bf16 split (FP32-accurate) + f64", "fp64": "f64"}
+DTYPES = {"learned": "bf16 digit planes (5 x 7-bit digits, products to ~5e-10) + f64",
+          "mixed": "bf16 digit planes (5 x 7-bit digits, products to ~5e-10) + f64", "fp64": "f64"}
 N512 = "gnp512_int10"
 
 
@@ -250,6 +253,41 @@ def n512_block(torch, M, stream, form, nodes=16, cap_s=60.0):
         tto[f] = rec
     out["time_capped_bab"] = tto
     return out
+
+
+TORUS = "torus20x20_pm1"
+
+
+def torus_block(torch, M, stream, form):
+    """The 2D toroidal spin glass (20 x 20, n = 400, +-1 weights, all three cut
+    families): the chosen form on the nodes whose oracle answers are stored with
+    the tests (tests/golden/oracle_fullsize.json, the oracle in the mode the GPU
+    reproduces), bounded together in one call with the stored incumbent; node
+    throughput and each node's relative difference from the oracle's bound.  The
+    plain FP64 form is left out here: one of these nodes takes minutes in it."""
+    from madam_gb300 import workload as W
+
+    fx = json.load(open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "tests", "golden",
+                                     "oracle_fullsize.json")))
+    recs = fx["workloads"][TORUS]
+    wl = W.make(TORUS)
+    prm = M.params(**wl["params"])
+    ctx = _context(M, prm, wl["SL"], wl["n"], len(recs), form, stream.cuda_stream, profile=False)
+    got = {}
+
+    def step():
+        ctx.set_trials(prm.Pent_Trials, prm.Hepta_Trials)
+        ctx.set_lb(fx["incumbent"][TORUS])
+        b, st = ctx.bound_batch([M.node(wl["fixings"][r["node"]]) for r in recs], rank=1)
+        got["b"], got["st"] = b, st
+        return st
+    d, w, st, _ = _time_steps(torch, ctx, step, stream, 1, 0)
+    ctx.close()
+    rel = [abs(b - r["bound"]) / abs(r["bound"]) for b, r in zip(got["b"], recs)]
+    return {"workload": TORUS, "n": wl["n"], "nodes": len(recs), "value": len(recs) / d, "unit": UNIT,
+            "steps": 1, "warmup": 0, "admm_iters": [s.admm_iters for s in got["st"]],
+            "oracle_admm_iters": [r["admm_iters"] for r in recs],
+            "bound_rel_diff_vs_oracle": rel}
 
 
 def uneven_block(torch, M, stream, form, count=2000, plain_count=128, batch=128):
@@ -437,7 +475,7 @@ def run_ours(a):
     roof = _roofline(M, ks, kw, a.workload)
     tot_ms = sum(x[1] for x in ks.values())
     share = {k: round(v[1] / max(1e-9, tot_ms), 4) for k, v in ks.items() if v[1] > 0}
-    plain = tto = n512 = uneven = None
+    plain = tto = n512 = uneven = torus = None
     if not a.no_compare and a.form != "fp64":
         # the plain FP64 form on the same workload (one warm-up, one timed step)
         pc = _context(M, prm, wl["SL"], wl["n"], batch, "fp64", stream.cuda_stream, profile=False)
@@ -462,6 +500,7 @@ def run_ours(a):
         tto["same_optimum"] = tto["fp64"]["optimum"] == tto[a.form]["optimum"]
         if a.workload != N512:
             n512 = n512_block(torch, M, stream, a.form)
+        torus = torus_block(torch, M, stream, a.form)
         uneven = uneven_block(torch, M, stream, a.form)
     cpu = None
     if not a.no_cpu_baseline:
@@ -495,6 +534,7 @@ def run_ours(a):
         "speedup_vs_plain_fp64": (plain["ms_per_step"] / (dev_s * 1e3 / a.steps)) if plain else None,
         "time_to_optimum": tto,
         "n512": n512,
+        "torus": torus,
         "uneven_batch": uneven,
         "cpu_baseline": cpu,
         "clocks": clk,
