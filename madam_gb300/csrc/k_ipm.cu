@@ -4,88 +4,62 @@
 // corrector for max <L,X> s.t. diag X = e, X psd) with one slot per node:
 // Cholesky factorisations, inverses, solves and the line searches run one CTA
 // per node; the two n^3 products Zi*tmp (ipm_mc_pk.c:181,249) run as a tiled
-// multi-CTA GEMM.  Iterates: X (s.X), y (s.y), Z = Diag(y) - L (s.Q),
+// multi-CTA FP64 GEMM.  Iterates: X (s.X), y (s.y), Z = Diag(y) - L (s.Q),
 // Zi (s.W), factor of Zi o X (s.T1), dX1 (s.V), dX (s.A), scratch (s.T2).
-//
-// Precision.  The iterates, the objective sums and the stopping test are FP64
-// throughout.  While the primal-dual gap phi - psi exceeds kIpmLoGap the
-// factorisations, inverse, solves, line-search tests and the two products run
-// in FP32 (the FP64 pipe of this part runs at 1/64 of the FP32 rate, and these
-// are 5 n^3 / 3 + 4 n^3 flops per iteration on one SM per node); the iterations
-// that close the gap to the reference's 1e-4 run in FP64, as the reference does.
-// Newton's method corrects the early steps' rounding: the FP64 iterations end at
-// the same point to rounding.  A slot whose FP32 factorisation of Z or of
-// Zi o X fails (loss of definiteness at FP32 rounding) redoes that iteration in
-// FP64 and stays in FP64.
-#include "../../include/mcbound.h"
 #include "mcb_dev.cuh"
 #include "kernels.h"
 
 namespace mcb {
 
-constexpr double kIpmLoGap = 0.1;  // FP32 arithmetic while phi - psi exceeds this
-
-// Cholesky A = L L^T (lower, in place) of the n x n matrix at A with one CTA, in
-// the arithmetic of R.  Returns 0 on success or k+1 for a non-positive pivot
-// (dpotrf's INFO).  The trailing update: warps take columns, lanes rows.
-template <typename R>
-__device__ int cta_cholesky(R *A, int n) {
+// Cholesky A = L L^T (lower, in place) of the n x n matrix at A with one CTA.
+// Returns 0 on success or k+1 for a non-positive pivot (dpotrf's INFO).
+__device__ int cta_cholesky(double *A, int n) {
     __shared__ int info;
-    __shared__ R piv;
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    __shared__ double piv;
     if (threadIdx.x == 0) info = 0;
     __syncthreads();
     for (int k = 0; k < n; ++k) {
         if (threadIdx.x == 0) {
-            R a = A[k + (size_t)k * n];
-            if (!(a > R(0))) info = k + 1;
+            double a = A[k + (size_t)k * n];
+            if (!(a > 0.0)) info = k + 1;
             piv = sqrt(a);
             A[k + (size_t)k * n] = piv;
         }
         __syncthreads();
         if (info) return info;
-        const R inv = R(1) / piv;
+        double inv = 1.0 / piv;
         for (int i = k + 1 + threadIdx.x; i < n; i += blockDim.x) A[i + (size_t)k * n] *= inv;
         __syncthreads();
-        for (int j = k + 1 + wid; j < n; j += nw) {
-            const R ajk = A[j + (size_t)k * n];
-            for (int i = j + lane; i < n; i += 32) A[i + (size_t)j * n] -= A[i + (size_t)k * n] * ajk;
+        const int m = n - k - 1;
+        for (int idx = threadIdx.x; idx < m * m; idx += blockDim.x) {
+            int jj = idx / m, ii = idx - jj * m;
+            if (ii < jj) continue;
+            int i = k + 1 + ii, j = k + 1 + jj;
+            A[i + (size_t)j * n] -= A[i + (size_t)k * n] * A[j + (size_t)k * n];
         }
         __syncthreads();
     }
     return 0;
 }
 
-// b <- (L L^T)^{-1} b with the lower factor L, whole CTA (column oriented), in
-// the arithmetic of R; FP32 solves work on a shared copy of b.
-template <typename R>
-__device__ void cta_chol_solve_r(const R *Lf, int n, R *b) {
+// b <- (L L^T)^{-1} b with the lower factor L, whole CTA (column oriented).
+__device__ void cta_chol_solve(const double *Lf, int n, double *b) {
     for (int k = 0; k < n; ++k) {
         __syncthreads();
-        R yk = b[k] / Lf[k + (size_t)k * n];
+        double yk = b[k] / Lf[k + (size_t)k * n];
         __syncthreads();
         if (threadIdx.x == 0) b[k] = yk;
         for (int i = k + 1 + threadIdx.x; i < n; i += blockDim.x) b[i] -= Lf[i + (size_t)k * n] * yk;
     }
     for (int k = n - 1; k >= 0; --k) {
         __syncthreads();
-        R xk = b[k] / Lf[k + (size_t)k * n];
+        double xk = b[k] / Lf[k + (size_t)k * n];
         __syncthreads();
         if (threadIdx.x == 0) b[k] = xk;
         for (int i = threadIdx.x; i < k; i += blockDim.x) b[i] -= Lf[k + (size_t)i * n] * xk;
     }
     __syncthreads();
 }
-__device__ void cta_chol_solve(const double *Lf, int n, double *b) { cta_chol_solve_r(Lf, n, b); }
-__shared__ float g_bf[MCB_NMAX];  // the FP32 solves' right-hand side
-__device__ void cta_chol_solve(const float *Lf, int n, double *b) {
-    for (int i = threadIdx.x; i < n; i += blockDim.x) g_bf[i] = (float)b[i];
-    cta_chol_solve_r(Lf, n, g_bf);
-    for (int i = threadIdx.x; i < n; i += blockDim.x) b[i] = (double)g_bf[i];
-    __syncthreads();
-}
-
-__device__ __forceinline__ bool ipm_lo(const Slot &s) { return s.acc[ACC_IPM_LO] != 0.0; }
 
 // ---------------------------------------------------------------------------
 // Initial point, ipm_mc_pk.c:57-91
@@ -122,7 +96,6 @@ __global__ void k_ipm_init(Slot *slots) {
         s.acc[ACC_IPM_IT] = 0;
         s.acc[ACC_IPM_INFO] = 0;
         s.acc[ACC_IPM_DONE] = (py - pl > 1e-4) ? 0.0 : 1.0;
-        s.acc[ACC_IPM_LO] = (py - pl > kIpmLoGap) ? 1.0 : 0.0;
         // a non-finite objective (NaN or overflow in L) cannot start the IPM
         if (!isfinite(py) || !isfinite(pl)) {
             s.acc[ACC_IPM_DONE] = 1.0;
@@ -134,48 +107,10 @@ __global__ void k_ipm_init(Slot *slots) {
 __device__ __forceinline__ bool ipm_live(const Slot &s) { return s.active && s.acc[ACC_IPM_DONE] == 0.0; }
 
 // Zi = Z^{-1} (ipm_mc_pk.c:121-142): A <- chol(Z); W <- inverse, full symmetric.
-// One thread per column of the inverse: forward and back substitution.
-template <typename R>
-__device__ void cta_inverse_cols(const R *Lf, int n, R *out) {
-    for (int c = threadIdx.x; c < n; c += blockDim.x) {
-        R *x = out + (size_t)c * n;
-        for (int i = 0; i < c; ++i) x[i] = R(0);
-        for (int i = c; i < n; ++i) {
-            R acc = i == c ? R(1) : R(0);
-            for (int k = c; k < i; ++k) acc -= Lf[i + (size_t)k * n] * x[k];
-            x[i] = acc / Lf[i + (size_t)i * n];
-        }
-        for (int i = n - 1; i >= 0; --i) {
-            R acc = x[i];
-            for (int k = i + 1; k < n; ++k) acc -= Lf[k + (size_t)i * n] * x[k];
-            x[i] = acc / Lf[i + (size_t)i * n];
-        }
-    }
-    __syncthreads();
-}
-
 __global__ void __launch_bounds__(512) k_ipm_inverse(Slot *slots) {
     Slot &s = slots[blockIdx.x];
     if (!ipm_live(s)) return;
     const int n = s.n;
-    if (ipm_lo(s)) {
-        // FP32: factor in A, inverse in T2 (scratch until the predictor), then W
-        float *Af = (float *)s.A, *Wf = (float *)s.T2;
-        for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) Af[idx] = (float)s.Q[idx];
-        __syncthreads();
-        if (cta_cholesky(Af, n) == 0) {
-            cta_inverse_cols(Af, n, Wf);
-            for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) {
-                int j = idx / n, i = idx - j * n;
-                s.W[idx] = i >= j ? 0.5 * ((double)Wf[idx] + (double)Wf[j + (size_t)i * n])
-                                  : 0.5 * ((double)Wf[j + (size_t)i * n] + (double)Wf[idx]);
-            }
-            return;
-        }
-        // Z is not definite at FP32 rounding: this iteration and the rest in FP64
-        if (threadIdx.x == 0) s.acc[ACC_IPM_LO] = 0.0;
-        __syncthreads();
-    }
     for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) s.A[idx] = s.Q[idx];
     __syncthreads();
     int info = cta_cholesky(s.A, n);
@@ -183,7 +118,22 @@ __global__ void __launch_bounds__(512) k_ipm_inverse(Slot *slots) {
         if (threadIdx.x == 0) { s.acc[ACC_IPM_INFO] = 1; s.acc[ACC_IPM_DONE] = 1; s.status = -4; }
         return;
     }
-    cta_inverse_cols(s.A, n, s.W);
+    const double *Lf = s.A;
+    for (int c = threadIdx.x; c < n; c += blockDim.x) {
+        double *x = s.W + (size_t)c * n;
+        for (int i = 0; i < c; ++i) x[i] = 0.0;
+        for (int i = c; i < n; ++i) {
+            double acc = i == c ? 1.0 : 0.0;
+            for (int k = c; k < i; ++k) acc -= Lf[i + (size_t)k * n] * x[k];
+            x[i] = acc / Lf[i + (size_t)i * n];
+        }
+        for (int i = n - 1; i >= 0; --i) {
+            double acc = x[i];
+            for (int k = i + 1; k < n; ++k) acc -= Lf[k + (size_t)i * n] * x[k];
+            x[i] = acc / Lf[i + (size_t)i * n];
+        }
+    }
+    __syncthreads();
     for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) {
         int j = idx / n, i = idx - j * n;
         if (i > j) {
@@ -200,30 +150,14 @@ __global__ void __launch_bounds__(512) k_ipm_predictor(Slot *slots) {
     Slot &s = slots[blockIdx.x];
     if (!ipm_live(s)) return;
     const int n = s.n;
+    for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) s.T1[idx] = s.W[idx] * s.X[idx];
     for (int i = threadIdx.x; i < n; i += blockDim.x) s.dy1[i] = -1.0;
-    bool done = false;
-    if (ipm_lo(s)) {
-        float *T1f = (float *)s.T1;
-        for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) T1f[idx] = (float)(s.W[idx] * s.X[idx]);
-        __syncthreads();
-        if (cta_cholesky(T1f, n) == 0) {
-            cta_chol_solve(T1f, n, s.dy1);
-            done = true;
-        } else {
-            // the corrector reads the factor's precision from the flag: FP64 from here
-            if (threadIdx.x == 0) s.acc[ACC_IPM_LO] = 0.0;
-            __syncthreads();
-        }
+    __syncthreads();
+    if (cta_cholesky(s.T1, n)) {
+        if (threadIdx.x == 0) { s.acc[ACC_IPM_INFO] = 2; s.acc[ACC_IPM_DONE] = 1; s.status = -4; }
+        return;
     }
-    if (!done) {
-        for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) s.T1[idx] = s.W[idx] * s.X[idx];
-        __syncthreads();
-        if (cta_cholesky(s.T1, n)) {
-            if (threadIdx.x == 0) { s.acc[ACC_IPM_INFO] = 2; s.acc[ACC_IPM_DONE] = 1; s.status = -4; }
-            return;
-        }
-        cta_chol_solve(s.T1, n, s.dy1);
-    }
+    cta_chol_solve(s.T1, n, s.dy1);
     for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) {
         int i = idx % n;
         s.T2[idx] = -(s.dy1[i]) * s.X[idx];
@@ -254,10 +188,7 @@ __global__ void __launch_bounds__(512) k_ipm_corrector(Slot *slots) {
         s.dy[i] = -r + mu * s.W[i + (size_t)i * n];
     }
     __syncthreads();
-    if (ipm_lo(s))
-        cta_chol_solve((const float *)s.T1, n, s.dy);
-    else
-        cta_chol_solve(s.T1, n, s.dy);
+    cta_chol_solve(s.T1, n, s.dy);
     for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) {
         int i = idx % n;
         double t1 = -(s.dy[i]) * s.X[idx];
@@ -273,7 +204,6 @@ __global__ void __launch_bounds__(512) k_ipm_step(Slot *slots) {
     if (!ipm_live(s)) return;
     const int n = s.n;
     const double mu = s.acc[ACC_MU];
-    const bool lo = ipm_lo(s);
     __shared__ double red[40];
     __shared__ double ap_s, ad_s;
     for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) {
@@ -298,16 +228,9 @@ __global__ void __launch_bounds__(512) k_ipm_step(Slot *slots) {
             if (threadIdx.x == 0) { s.acc[ACC_IPM_INFO] = 3; s.acc[ACC_IPM_DONE] = 1; s.status = -6; }
             return;
         }
-        if (lo) {
-            float *T2f = (float *)s.T2;
-            for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) T2f[idx] = (float)(s.X[idx] + ap * s.A[idx]);
-            __syncthreads();
-            if (cta_cholesky(T2f, n) == 0) break;
-        } else {
-            for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) s.T2[idx] = s.X[idx] + ap * s.A[idx];
-            __syncthreads();
-            if (cta_cholesky(s.T2, n) == 0) break;
-        }
+        for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) s.T2[idx] = s.X[idx] + ap * s.A[idx];
+        __syncthreads();
+        if (cta_cholesky(s.T2, n) == 0) break;
         ap *= 0.8;
     }
     if (ap < 1.0) ap *= 0.95;
@@ -317,22 +240,12 @@ __global__ void __launch_bounds__(512) k_ipm_step(Slot *slots) {
             if (threadIdx.x == 0) { s.acc[ACC_IPM_INFO] = 4; s.acc[ACC_IPM_DONE] = 1; s.status = -6; }
             return;
         }
-        if (lo) {
-            float *T2f = (float *)s.T2;
-            for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) {
-                int j = idx / n, i = idx - j * n;
-                T2f[idx] = (float)(s.Q[idx] + (i == j ? ad * s.dy[i] : 0.0));
-            }
-            __syncthreads();
-            if (cta_cholesky(T2f, n) == 0) break;
-        } else {
-            for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) {
-                int j = idx / n, i = idx - j * n;
-                s.T2[idx] = s.Q[idx] + (i == j ? ad * s.dy[i] : 0.0);
-            }
-            __syncthreads();
-            if (cta_cholesky(s.T2, n) == 0) break;
+        for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) {
+            int j = idx / n, i = idx - j * n;
+            s.T2[idx] = s.Q[idx] + (i == j ? ad * s.dy[i] : 0.0);
         }
+        __syncthreads();
+        if (cta_cholesky(s.T2, n) == 0) break;
         ad *= 0.8;
     }
     if (ad < 1.0) ad *= 0.95;
@@ -366,36 +279,36 @@ __global__ void __launch_bounds__(512) k_ipm_step(Slot *slots) {
         s.acc[ACC_AD] = ad;
         s.acc[ACC_IPM_IT] += 1.0;
         if (!(py - pl > 1e-4)) s.acc[ACC_IPM_DONE] = 1.0;
-        // once in FP64, the rest of the run stays there
-        if (!(py - pl > kIpmLoGap)) s.acc[ACC_IPM_LO] = 0.0;
         if (s.acc[ACC_IPM_IT] >= 500) { s.acc[ACC_IPM_DONE] = 1.0; s.status = -6; }
     }
 }
 
 // ---------------------------------------------------------------------------
-// Batched GEMM, C = A * B for the IPM products (square n x n per slot), FP64
-// storage, in FP32 or FP64 arithmetic by the slot's precision flag.
+// Batched FP64 GEMM, C = A * B for the IPM products (square n x n per slot).
 // which: 0 -> V = W * T2 ; 1 -> A = W * T2.  64x64 tiles, 256 threads, 4x4 per thread.
-template <typename R>
-__device__ void ipm_gemm_tile(Slot &s, int which, int i0, int j0) {
+__global__ void __launch_bounds__(256) k_ipm_gemm(Slot *slots, int which) {
+    Slot &s = slots[blockIdx.z];
+    if (!ipm_live(s)) return;
     const int n = s.n;
+    const int i0 = blockIdx.y * 64, j0 = blockIdx.x * 64;
+    if (i0 >= n || j0 >= n) return;
     const double *Am = s.W, *Bm = s.T2;
     double *Cm = which == 0 ? s.V : s.A;
-    __shared__ R As[16][64 + 1], Bs[16][64 + 1];
+    __shared__ double As[16][64 + 1], Bs[16][64 + 1];
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-    R acc[4][4] = {};
+    double acc[4][4] = {};
     for (int k0 = 0; k0 < n; k0 += 16) {
         for (int q = threadIdx.x; q < 16 * 64; q += 256) {
             int r = q & 63, kk = q >> 6;
             int ia = i0 + r, ka = k0 + kk;
-            As[kk][r] = (ia < n && ka < n) ? (R)Am[ia + (size_t)ka * n] : R(0);
+            As[kk][r] = (ia < n && ka < n) ? Am[ia + (size_t)ka * n] : 0.0;
             int kb = k0 + (q & 15), jb = j0 + (q >> 4);
-            Bs[q & 15][q >> 4] = (kb < n && jb < n) ? (R)Bm[kb + (size_t)jb * n] : R(0);
+            Bs[q & 15][q >> 4] = (kb < n && jb < n) ? Bm[kb + (size_t)jb * n] : 0.0;
         }
         __syncthreads();
 #pragma unroll
         for (int kk = 0; kk < 16; ++kk) {
-            R a[4], b[4];
+            double a[4], b[4];
 #pragma unroll
             for (int r = 0; r < 4; ++r) a[r] = As[kk][ty * 4 + r];
 #pragma unroll
@@ -412,19 +325,8 @@ __device__ void ipm_gemm_tile(Slot &s, int which, int i0, int j0) {
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
             int i = i0 + ty * 4 + r, j = j0 + tx * 4 + c;
-            if (i < n && j < n) Cm[i + (size_t)j * n] = (double)acc[r][c];
+            if (i < n && j < n) Cm[i + (size_t)j * n] = acc[r][c];
         }
-}
-__global__ void __launch_bounds__(256) k_ipm_gemm(Slot *slots, int which) {
-    Slot &s = slots[blockIdx.z];
-    if (!ipm_live(s)) return;
-    const int n = s.n;
-    const int i0 = blockIdx.y * 64, j0 = blockIdx.x * 64;
-    if (i0 >= n || j0 >= n) return;
-    if (ipm_lo(s))
-        ipm_gemm_tile<float>(s, which, i0, j0);
-    else
-        ipm_gemm_tile<double>(s, which, i0, j0);
 }
 
 // ---------------------------------------------------------------------------

@@ -68,7 +68,6 @@ enum Acc {
     ACC_MU, ACC_PHI, ACC_PSI, ACC_AP, ACC_AD, ACC_IPM_IT, ACC_IPM_DONE, ACC_IPM_INFO,
     // Newton-Schulz projection: scale of W and trace of sign(W)
     ACC_NS_ALPHA, ACC_NS_TRACE,
-    ACC_IPM_LO,       // 1 while this IPM iteration factors and multiplies in FP32
     kAcc = 32
 };
 
