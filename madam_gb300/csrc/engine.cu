@@ -461,7 +461,7 @@ int launch_admm_iteration(mcb_ctx *c, int ns, int mmax, int emax) {
         // to rounding); the Newton-Schulz forms carry projection errors of ~5e-9 of
         // ||W||, so a 1e-10 solve stays below them
         Prof p(c, K_CG, 1);
-        launch_cg(d, ns, c->cg_max_iters, c->proj == MCB_PROJ_FP64 ? 1e-13 : 1e-10, c->st);
+        launch_cg(d, ns, mmax, c->cg_max_iters, c->proj == MCB_PROJ_FP64 ? 1e-13 : 1e-10, c->st);
     }
     { Prof p(c, K_SU, 1); launch_admm_su(d, ns, mmax, c->st); }
     { Prof p(c, K_W, 2); launch_build_W(d, ns, N, emax, 0, c->st); }
@@ -1539,6 +1539,10 @@ mcb_ctx *mcb_create(const mcb_params *params, int N, const double *SL, int batch
     if (rc == MCB_OK) chk(cudaMalloc(&c->d_tbnd, (size_t)batch_max * c->tcap_bnd * sizeof(unsigned int)));
     if (rc == MCB_OK) chk(cudaMalloc(&c->d_tbndv, (size_t)batch_max * c->tcap_bnd * sizeof(double)));
     c->proj = proj;
+    if (rc == MCB_OK && cg_prepare()) {
+        rc = MCB_ERR_CUDA;
+        c->err = "CG kernel attributes";
+    }
     if (rc == MCB_OK && proj != MCB_PROJ_FP64) {
         rc = c->ns.init(proj, N, batch_max, c->st);
         if (rc != MCB_OK) c->err = "Newton-Schulz buffers or cuBLAS handle";

@@ -26,7 +26,9 @@ void launch_ipm_iteration(Slot *d, int ns, int nmax, cudaStream_t st);
 
 // k_admm.cu
 void launch_admm_rhs(Slot *d, int ns, int nmax, int mmax, cudaStream_t st);
-void launch_cg(Slot *d, int ns, int maxit, double rtol, cudaStream_t st);
+// k_cg's shared-memory limit (once per device, before any launch or capture); 0 on success
+int cg_prepare();
+void launch_cg(Slot *d, int ns, int mmax, int maxit, double rtol, cudaStream_t st);
 // the FP32 copy of every active slot's (B B^T + I) values (after an upload of the system)
 void launch_cg_values(Slot *d, int ns, cudaStream_t st);
 void launch_admm_su(Slot *d, int ns, int mmax, cudaStream_t st);

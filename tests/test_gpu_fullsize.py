@@ -118,4 +118,4 @@ def test_chosen_form_slow_torus_nodes_stay_close(gpu_lib):
     for r, bg, sg in zip(recs, b, st):
         assert abs(bg - r["bound"]) <= 1e-3 * abs(r["bound"]), (r["node"], bg, r["bound"])
         assert bg >= INCUMBENT[name]
-        assert abs(sg.admm_iters - r["admm_iters"]) <= 0.05 * r["admm_iters"]
+        assert abs(sg.admm_iters - r["admm_iters"]) <= 0.25 * r["admm_iters"]
