@@ -66,59 +66,61 @@ __global__ void k_admm_rhs(Slot *slots) {
 // r = rhs - A t and the stopping test in FP64, the correction A d = r by
 // conjugate gradients in FP32 (its rate is ~64x FP64's on this part) to 1e-5 of
 // ||r||, then t += d.  A has eigenvalues in [1, ~11], so each outer step gains
-// about five digits and two or three reach 1e-13.  One CTA per slot.  The
-// products take a group of kCgGroup lanes per matrix row (CSR rows hold ~20-60
-// entries: the lanes read a row's entries together and add their partial sums by
-// shuffles), and the element-wise updates of row i run on the lane that made q_i.
-// The FP32 work vectors (direction p, product q, scaled residual, correction)
-// live in shared memory when the slot has at most sh_cap cuts, otherwise in the
-// slot's cgp / cgq arrays (two floats per double).  The FP32 copy of A's values
-// is g_v32.  The iteration cap counts the FP32 CG iterations; reaching it before
-// the tolerance sets status and leaves t as far as it got.
-constexpr int kCgOuter = 12;           // refinement steps at most
-constexpr double kCgInnerRel2 = 1e-10;  // (1e-5)^2: the inner CG's relative target
-constexpr int kCgGroup = 8;             // lanes per matrix row in the products
-constexpr int kCgShMax = 8192;          // cuts whose FP32 vectors fit in shared memory (128 KB)
-template <typename T>
-__device__ __forceinline__ T group_sum(T v) {
-#pragma unroll
-    for (int o = kCgGroup / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o, kCgGroup);
-    return v;
-}
-__global__ void __launch_bounds__(1024) k_cg(Slot *slots, int maxit, double rtol2, int sh_cap) {
+// about five digits and two or three reach 1e-13.  One CTA per slot, one thread
+// per matrix row.  The system is small and fixed for the whole solve (m cuts,
+// a few nonzeros per row), so the solve is a chain of short, synchronised
+// steps whose cost is latency: the kernel copies the CSR structure and the FP32
+// values into shared memory once, next to the FP32 work vectors (direction p,
+// product q, scaled residual, correction), when they fit in kCgShBytes; the
+// vectors alone when only they fit; otherwise everything stays in the slot's
+// arrays (cgp / cgq hold two floats per double).  The iteration cap counts the
+// FP32 CG iterations; reaching it before the tolerance sets status and leaves t
+// as far as it got.
+constexpr int kCgOuter = 12;             // refinement steps at most
+constexpr double kCgInnerRel2 = 1e-10;   // (1e-5)^2: the inner CG's relative target
+constexpr int kCgShBytes = 200 * 1024;   // dynamic shared memory of k_cg
+__global__ void __launch_bounds__(1024) k_cg(Slot *slots, int maxit, double rtol2) {
     Slot &s = slots[blockIdx.x];
     if (!live(s)) return;
     const int m = s.m;
     if (m == 0) return;
     __shared__ double red[40];
-    extern __shared__ float csh[];  // 4 sh_cap floats
-    const bool in_sh = m <= sh_cap;
+    extern __shared__ float csh[];
+    const int nnz = s.g_rp[m];
+    const size_t vec_words = 4 * (size_t)m, csr_words = (size_t)m + 1 + 2 * (size_t)nnz;
+    const bool vec_sh = vec_words * 4 <= kCgShBytes, csr_sh = (vec_words + csr_words) * 4 <= kCgShBytes;
     double *x = s.t, *r = s.cgr;
-    float *p = in_sh ? csh : (float *)s.cgq, *q = in_sh ? csh + sh_cap : (float *)s.cgq + m;
-    float *ri = in_sh ? csh + 2 * sh_cap : (float *)s.cgp, *d = in_sh ? csh + 3 * sh_cap : (float *)s.cgp + m;
+    float *p = vec_sh ? csh : (float *)s.cgq, *q = vec_sh ? csh + m : (float *)s.cgq + m;
+    float *ri = vec_sh ? csh + 2 * m : (float *)s.cgp, *d = vec_sh ? csh + 3 * m : (float *)s.cgp + m;
     const int *rp = s.g_rp, *ci = s.g_ci;
-    const double *gv = s.g_v;
     const float *gf = s.g_v32;
-    const int g = threadIdx.x / kCgGroup, gl = threadIdx.x % kCgGroup, ng = blockDim.x / kCgGroup;
+    if (csr_sh) {
+        int *rps = (int *)(csh + vec_words), *cis = rps + m + 1;
+        float *gfs = (float *)(cis + nnz);
+        for (int k = threadIdx.x; k <= m; k += blockDim.x) rps[k] = s.g_rp[k];
+        for (int k = threadIdx.x; k < nnz; k += blockDim.x) {
+            cis[k] = s.g_ci[k];
+            gfs[k] = s.g_v32[k];
+        }
+        rp = rps;
+        ci = cis;
+        gf = gfs;
+    }
+    const double *gv = s.g_v;
     double lbb = 0.0;
     for (int i = threadIdx.x; i < m; i += blockDim.x) lbb += s.rhs[i] * s.rhs[i];
-    const double bb = block_sum(lbb, red);
+    const double bb = block_sum(lbb, red);  // (its barriers also publish the copies above)
     const double stop2 = rtol2 * bb;
     int it = 0;
     double rr = 0.0;
     for (int outer = 0;; ++outer) {
         double lrr = 0.0;
-        for (int i0 = 0; i0 < m; i0 += ng) {  // warp-uniform trip count (shuffles)
-            const int i = i0 + g;
+        for (int i = threadIdx.x; i < m; i += blockDim.x) {
             double acc = 0.0;
-            if (i < m)
-                for (int k = rp[i] + gl; k < rp[i + 1]; k += kCgGroup) acc += gv[k] * x[ci[k]];
-            acc = group_sum(acc);
-            if (i < m && gl == 0) {
-                const double res = s.rhs[i] - acc;
-                r[i] = res;
-                lrr += res * res;
-            }
+            for (int k = rp[i]; k < rp[i + 1]; ++k) acc += gv[k] * x[ci[k]];
+            const double res = s.rhs[i] - acc;
+            r[i] = res;
+            lrr += res * res;
         }
         rr = block_sum(lrr, red);
         if (rr <= stop2 || it >= maxit || outer >= kCgOuter) break;
@@ -134,21 +136,16 @@ __global__ void __launch_bounds__(1024) k_cg(Slot *slots, int maxit, double rtol
         double rz = 1.0;  // the scaled residual's squared norm
         while (rz > kCgInnerRel2 && it < maxit) {
             double lpq = 0.0;
-            for (int i0 = 0; i0 < m; i0 += ng) {
-                const int i = i0 + g;
+            for (int i = threadIdx.x; i < m; i += blockDim.x) {
                 float acc = 0.0f;
-                if (i < m)
-                    for (int k = rp[i] + gl; k < rp[i + 1]; k += kCgGroup) acc = fmaf(gf[k], p[ci[k]], acc);
-                acc = group_sum(acc);
-                if (i < m && gl == 0) {
-                    q[i] = acc;
-                    lpq += (double)(p[i] * acc);
-                }
+                for (int k = rp[i]; k < rp[i + 1]; ++k) acc = fmaf(gf[k], p[ci[k]], acc);
+                q[i] = acc;
+                lpq += (double)(p[i] * acc);
             }
             const double pq = block_sum(lpq, red);
             const float alpha = (float)(rz / pq);
             double l2 = 0.0;
-            for (int i = g; i < m && gl == 0; i += ng) {
+            for (int i = threadIdx.x; i < m; i += blockDim.x) {
                 d[i] = fmaf(alpha, p[i], d[i]);
                 const float v = fmaf(-alpha, q[i], ri[i]);
                 ri[i] = v;
@@ -156,7 +153,7 @@ __global__ void __launch_bounds__(1024) k_cg(Slot *slots, int maxit, double rtol
             }
             const double rz2 = block_sum(l2, red);
             const float beta = (float)(rz2 / rz);
-            for (int i = g; i < m && gl == 0; i += ng) p[i] = fmaf(beta, p[i], ri[i]);
+            for (int i = threadIdx.x; i < m; i += blockDim.x) p[i] = fmaf(beta, p[i], ri[i]);
             __syncthreads();
             rz = rz2;
             ++it;
@@ -353,14 +350,12 @@ void launch_admm_rhs(Slot *d, int ns, int nmax, int mmax, cudaStream_t st) {
     k_admm_rhs<<<g, 256, 0, st>>>(d);
 }
 int cg_prepare() {
-    return cudaFuncSetAttribute(k_cg, cudaFuncAttributeMaxDynamicSharedMemorySize, 4 * kCgShMax * (int)sizeof(float)) ==
-                   cudaSuccess
-               ? 0
-               : -1;
+    return cudaFuncSetAttribute(k_cg, cudaFuncAttributeMaxDynamicSharedMemorySize, kCgShBytes) == cudaSuccess ? 0
+                                                                                                                : -1;
 }
 void launch_cg(Slot *d, int ns, int mmax, int maxit, double rtol, cudaStream_t st) {
-    const int cap = mmax < kCgShMax ? (mmax > 1 ? mmax : 1) : kCgShMax;
-    k_cg<<<ns, 1024, 4 * (size_t)cap * sizeof(float), st>>>(d, maxit, rtol * rtol, cap);
+    (void)mmax;
+    k_cg<<<ns, 1024, kCgShBytes, st>>>(d, maxit, rtol * rtol);
 }
 void launch_cg_values(Slot *d, int ns, cudaStream_t st) { k_cg_values<<<dim3(64, ns), 256, 0, st>>>(d); }
 void launch_admm_su(Slot *d, int ns, int mmax, cudaStream_t st) {
