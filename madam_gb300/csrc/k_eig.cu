@@ -586,7 +586,9 @@ __global__ void __launch_bounds__(256) k_syrk_post(Slot *slots, int mode, double
     const int i0 = ti * TS, j0 = tj * TS;
     __shared__ double Ya[16][TS + 1], Yb[16][TS + 1];
     __shared__ double red[40];
-    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8 threads, 4 rows each
+    // 32 x 8 threads: lane tx takes row i0 + tx (the column-major reads and the
+    // direct writes coalesce across the warp), four columns j0 + 4 ty + r each
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
     double acc[4] = {0, 0, 0, 0};
     const double *Y = s.V;
     for (int k0 = 0; k0 < M; k0 += 16) {
@@ -599,16 +601,16 @@ __global__ void __launch_bounds__(256) k_syrk_post(Slot *slots, int mode, double
         __syncthreads();
 #pragma unroll
         for (int kk = 0; kk < 16; ++kk) {
-            double bj = Yb[kk][tx];
+            const double ai = Ya[kk][tx];
 #pragma unroll
-            for (int r = 0; r < 4; ++r) acc[r] += Ya[kk][ty * 4 + r] * bj;
+            for (int r = 0; r < 4; ++r) acc[r] += ai * Yb[kk][ty * 4 + r];
         }
         __syncthreads();
     }
     double p_dres = 0.0, p_primal = 0.0, p_diag = 0.0;
     const double sg = s.sigma;
     for (int r = 0; r < 4; ++r) {
-        int i = i0 + ty * 4 + r, j = j0 + tx;
+        int i = i0 + tx, j = j0 + ty * 4 + r;
         if (i >= n || j >= n || i < j) continue;
         size_t ij = i + (size_t)j * n, ji = j + (size_t)i * n;
         double w = s.W[ij];

@@ -61,6 +61,8 @@ constexpr int kTileBytes = BM * BK * 2;                // one plane of one opera
 constexpr int kStageBytes = 2 * kPieces * kTileBytes;  // A and B, five planes each (80 KB)
 constexpr int kThreads = 256;                          // eight warps
 constexpr int kChunk = 16;                             // epilogue: columns per tcgen05.ld
+constexpr int kLdF = BM + 1;                           // epilogue staging F[c][r], in float pairs
+constexpr int kEpiBytes = BN * kLdF * 8;               // 132,096 B: the whole tile as float pairs
 __host__ __device__ constexpr int cmax(int a, int b) { return a > b ? a : b; }
 // variant 0: two stages; variant 1: one stage.  The four accumulators hold all 512
 // tensor-memory columns, so the shared memory asked for is at least kOneCtaBytes,
@@ -68,7 +70,7 @@ __host__ __device__ constexpr int cmax(int a, int b) { return a > b ? a : b; }
 constexpr int kStages0 = 2, kStages1 = 1;
 constexpr int kOneCtaBytes = 120 * 1024;
 constexpr int smem_bytes(int stages) {
-    return cmax(stages * kStageBytes + 1024 + 128, kOneCtaBytes);
+    return cmax(cmax(stages * kStageBytes, kEpiBytes) + 1024 + 128, kOneCtaBytes);
 }
 constexpr int kAccs = 4;
 constexpr uint32_t kTmemCols = kAccs * BN;   // 512: acc0 .. acc3
@@ -235,7 +237,7 @@ __global__ void __launch_bounds__(kThreads, 1)
               float diag, float in_scale, int sym, long long spin_limit, int issue_loads) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    uint64_t *full = (uint64_t *)(smem + kStages * kStageBytes);
+    uint64_t *full = (uint64_t *)(smem + cmax(kStages * kStageBytes, kEpiBytes));
     uint64_t *empty = full + kStages;
     uint64_t *done = empty + kStages;
     uint32_t *tmem_slot = (uint32_t *)(done + 1);
@@ -343,30 +345,33 @@ __global__ void __launch_bounds__(kThreads, 1)
         const float coef = alpha * in_scale;
         const double fscale = out.slot_scale ? out.slot_scale[slot] : 1.0;
         const int g = warp & 3;         // tensor-memory lanes 32 g .. 32 g + 31: tile rows
-        const int r = g * 32 + lane;    // this thread's tile row
-        const int row = m0 + r;
+        const int r = g * 32 + lane;    // this thread's tile row (phase A) / row of its output (phase B)
+        const int cbeg = (warp >> 2) * (BN / 2);
         const bool diag_tile = sym && ti == tj;
         const size_t sb = (size_t)slot * out.stride;
         const bool want_planes = out.p[0] != nullptr;
-        for (int c0 = (warp >> 2) * (BN / 2); c0 < (warp >> 2) * (BN / 2) + BN / 2; c0 += kChunk) {
-            float h[kChunk], l[kChunk];
-            {
-                float v[kAccs][kChunk];
+        // F[c kLdF + rr] = C(m0 + rr, n0 + c) as a float pair: the stage buffers are free
+        // once the MMAs are done
+        float2 *F = (float2 *)smem;
+        // the outputs of 16 consecutive columns of one output row at element offset o,
+        // from their float pairs: whole 32-byte sectors per thread
+        auto store_row = [&](size_t o, const float *h, const float *l) {
+            if (out.f32) {
+                float4 *o4 = reinterpret_cast<float4 *>(out.f32 + o);
 #pragma unroll
-                for (int a = 0; a < kAccs; ++a)
-                    tmem_ld16(tmem + ((uint32_t)(g * 32) << 16) + (uint32_t)(a * BN + c0), v[a]);
-#pragma unroll
-                for (int j = 0; j < kChunk; ++j) {
-                    const int col = n0 + c0 + j;
-                    const float2 x =
-                        ff_value(v[0][j], v[1][j], v[2][j], v[3][j], coef, (row == col && row < n) ? diag : 0.0f);
-                    h[j] = x.x;
-                    l[j] = x.y;
-                }
+                for (int q = 0; q < kChunk / 4; ++q)
+                    o4[q] = make_float4(h[4 * q] + l[4 * q], h[4 * q + 1] + l[4 * q + 1], h[4 * q + 2] + l[4 * q + 2],
+                                        h[4 * q + 3] + l[4 * q + 3]);
             }
-            // the element's digit planes, packed in pairs of consecutive columns
-            uint32_t pk[kPieces][kChunk / 2];
+            if (out.f64) {
+                double2 *o2 = reinterpret_cast<double2 *>(out.f64 + o);
+#pragma unroll
+                for (int q = 0; q < kChunk / 2; ++q)
+                    o2[q] = make_double2(fscale * ((double)h[2 * q] + (double)l[2 * q]),
+                                         fscale * ((double)h[2 * q + 1] + (double)l[2 * q + 1]));
+            }
             if (want_planes) {
+                uint32_t pk[kPieces][kChunk / 2];
 #pragma unroll
                 for (int j = 0; j < kChunk; j += 2) {
                     float d0[kPieces], d1[kPieces];
@@ -375,62 +380,54 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll
                     for (int p = 0; p < kPieces; ++p) pk[p][j / 2] = pack_bf16(d0[p], d1[p]);
                 }
-            }
-            // this row's 16 columns; a diagonal tile stores its own lower triangle
-            // (col <= row) element by element, and every element of a symmetric
-            // product goes to its mirror too (col < row on a diagonal tile); lanes are
-            // consecutive rows, so a mirror store is consecutive across the warp
-            const size_t od = sb + (size_t)row * npad + n0 + c0;
-            const size_t om = sb + (size_t)(n0 + c0) * npad + row;  // mirror of column c0
-            auto own = [&](int j) { return diag_tile && c0 + j <= r; };
-            auto mirror = [&](int j) { return sym && (!diag_tile || c0 + j < r); };
-            if (out.f32) {
-                float f[kChunk];
-#pragma unroll
-                for (int j = 0; j < kChunk; ++j) f[j] = h[j] + l[j];
-                if (!diag_tile) {
-                    float4 *o4 = reinterpret_cast<float4 *>(out.f32 + od);
-#pragma unroll
-                    for (int q = 0; q < kChunk / 4; ++q) o4[q] = make_float4(f[4 * q], f[4 * q + 1], f[4 * q + 2], f[4 * q + 3]);
-                }
-#pragma unroll
-                for (int j = 0; j < kChunk; ++j) {
-                    if (own(j)) out.f32[od + j] = f[j];
-                    if (mirror(j)) out.f32[om + (size_t)j * npad] = f[j];
-                }
-            }
-            if (out.f64) {
-                double dv[kChunk];
-#pragma unroll
-                for (int j = 0; j < kChunk; ++j) dv[j] = fscale * ((double)h[j] + (double)l[j]);
-                if (!diag_tile) {
-                    double2 *o2 = reinterpret_cast<double2 *>(out.f64 + od);
-#pragma unroll
-                    for (int q = 0; q < kChunk / 2; ++q) o2[q] = make_double2(dv[2 * q], dv[2 * q + 1]);
-                }
-#pragma unroll
-                for (int j = 0; j < kChunk; ++j) {
-                    if (own(j)) out.f64[od + j] = dv[j];
-                    if (mirror(j)) out.f64[om + (size_t)j * npad] = dv[j];
-                }
-            }
-            if (want_planes) {
 #pragma unroll
                 for (int p = 0; p < kPieces; ++p) {
-                    __nv_bfloat16 *o = out.p[p];
-                    if (!diag_tile) {
-                        uint4 *o4 = reinterpret_cast<uint4 *>(o + od);
-                        o4[0] = make_uint4(pk[p][0], pk[p][1], pk[p][2], pk[p][3]);
-                        o4[1] = make_uint4(pk[p][4], pk[p][5], pk[p][6], pk[p][7]);
-                    }
-#pragma unroll
-                    for (int j = 0; j < kChunk; ++j) {
-                        const uint32_t w = pk[p][j / 2];
-                        const __nv_bfloat16 b = __ushort_as_bfloat16((unsigned short)((j & 1) ? (w >> 16) : (w & 0xffffu)));
-                        if (own(j)) o[od + j] = b;
-                        if (mirror(j)) o[om + (size_t)j * npad] = b;
-                    }
+                    uint4 *o4 = reinterpret_cast<uint4 *>(out.p[p] + o);
+                    o4[0] = make_uint4(pk[p][0], pk[p][1], pk[p][2], pk[p][3]);
+                    o4[1] = make_uint4(pk[p][4], pk[p][5], pk[p][6], pk[p][7]);
                 }
+            }
+        };
+        // phase A: the accumulators of this thread's row, 16 columns at a time, summed to
+        // float pairs; an off-diagonal tile stores them in place, and a symmetric product
+        // stages them (transposed) for phase B
+        for (int c0 = cbeg; c0 < cbeg + BN / 2; c0 += kChunk) {
+            float h[kChunk], l[kChunk];
+            {
+                float v[kAccs][kChunk];
+#pragma unroll
+                for (int a = 0; a < kAccs; ++a)
+                    tmem_ld16(tmem + ((uint32_t)(g * 32) << 16) + (uint32_t)(a * BN + c0), v[a]);
+#pragma unroll
+                for (int j = 0; j < kChunk; ++j) {
+                    const int row = m0 + r, col = n0 + c0 + j;
+                    const float2 x =
+                        ff_value(v[0][j], v[1][j], v[2][j], v[3][j], coef, (row == col && row < n) ? diag : 0.0f);
+                    h[j] = x.x;
+                    l[j] = x.y;
+                    if (sym) F[(c0 + j) * kLdF + r] = x;
+                }
+            }
+            if (!diag_tile) store_row(sb + (size_t)(m0 + r) * npad + n0 + c0, h, l);
+        }
+        if (sym) {
+            __syncthreads();
+            // phase B: a diagonal tile writes its rows whole, each element taken from the
+            // lower triangle (C(c, r) for c > r), so the result is exactly symmetric; an
+            // off-diagonal tile writes its mirror: output row n0 + r holds C(m0 + k, n0 + r)
+            for (int c0 = cbeg; c0 < cbeg + BN / 2; c0 += kChunk) {
+                float h[kChunk], l[kChunk];
+#pragma unroll
+                for (int j = 0; j < kChunk; ++j) {
+                    const int c = c0 + j;
+                    const float2 x = diag_tile ? (c <= r ? F[c * kLdF + r] : F[r * kLdF + c]) : F[r * kLdF + c];
+                    h[j] = x.x;
+                    l[j] = x.y;
+                }
+                if (diag_tile)
+                    store_row(sb + (size_t)(m0 + r) * npad + n0 + c0, h, l);
+                else
+                    store_row(sb + (size_t)(n0 + r) * npad + m0 + c0, h, l);
             }
         }
     }
@@ -455,15 +452,11 @@ __global__ void k_tc_split(const T *src, size_t sstride, TcOut out, int npad, co
         if (sizeof(T) == 4 && !slot_div) {
             planes((float)s[q] * out.pscale, 0.0f, pl);  // a power-of-two scale: exact
         } else {
-            // FP64 remainders: each digit subtraction and the times-2^7 are exact
-            double x = (double)s[q] * inv * (double)out.pscale, w = 1.0;
-#pragma unroll
-            for (int a = 0; a < kPieces; ++a) {
-                const double d = rint(x);
-                pl[a] = __float2bfloat16_rn((float)(d * w));
-                x = (x - d) * 128.0;
-                w *= 1.0 / 128.0;
-            }
+            // the FP64 value as a float pair (h + l to 2^-48), then the digits in FP32:
+            // three FP64 operations per element instead of four per digit
+            const double x = (double)s[q] * inv * (double)out.pscale;
+            const float h = (float)x;
+            planes(h, (float)(x - (double)h), pl);
         }
 #pragma unroll
         for (int p = 0; p < kPieces; ++p) out.p[p][o] = pl[p];
