@@ -137,7 +137,8 @@ void mcb_get_trials(const mcb_ctx *ctx, int *pent_trials, int *hepta_trials);
  * eigenvalues change X+ by at most l0 ||W||_F / 2 each).  MCB_ERR_ARG on the FP64 form. */
 int mcb_ns_options(mcb_ctx *ctx, int operands, double l0);
 /* the Newton-Schulz step schedule of the context: count, and per step a, b of
- * S <- a S + b S^3 and whether its operands are FP32-accurate */
+ * S <- a S + b S^3 and whether it is a closing step (l > 0.9, the plain cubic;
+ * with MCB_NS_OPERANDS_NATIVE these run on accurate operands) */
 int mcb_ns_schedule(const mcb_ctx *ctx, int cap, float *a, float *b, int *accurate);
 /* the default schedule (safety 2%, closing within 1e-7 of 1) for a given l0; host
  * arithmetic only, callable without a device.  Returns the step count or MCB_ERR_ARG. */

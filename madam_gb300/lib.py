@@ -515,7 +515,7 @@ def project_noalloc(n, W_dev, Xp_dev, Q_dev, Z_dev, evals_dev, stream=None):
 
 
 def ns_schedule_for(l0=1e-6):
-    """The Newton-Schulz step schedule (a, b, FP32-accurate) for l0; needs no device."""
+    """The Newton-Schulz step schedule (a, b, closing step) for l0; needs no device."""
     cap = 64
     a, b, acc = (C.c_float * cap)(), (C.c_float * cap)(), (C.c_int * cap)()
     k = lib().mcb_ns_schedule_for(l0, cap, C.cast(a, C.c_void_p), C.cast(b, C.c_void_p), C.cast(acc, C.c_void_p))
