@@ -220,8 +220,8 @@ int mcb_project_psd(int n, const double *W, int proj, double *Xp, double *Q, dou
  * loads the library, for as long as it stays loaded).  Larger n returns
  * MCB_ERR_ARG.  Runs on `stream` and returns after it completes, with M on the
  * host.  The first call on a device looks up the scratch's device address
- * (cudaGetSymbolAddress); make that first call before any stream capture.
- * Calls share the scratch: calls that overlap on the GPU race. */
+ * (cudaGetSymbolAddress).  Calls share the scratch: calls that overlap on the
+ * GPU race. */
 #define MCB_NOALLOC_MAX_N 512
 int mcb_project_psd_noalloc(int n, const double *W, double *Xp, double *Q, double *Z, double *evals, int *M,
                             void *stream);
