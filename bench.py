@@ -534,7 +534,9 @@ def run_ours(a):
         "graphs": {"captured": graphs[0], "replayed": graphs[1]},
         "host_phase_seconds_per_step": host,
         "autotune": tune,
-        "roofline_step": "kernel shares and roofline from one extra step with per-class CUDA events",
+        "roofline_step": "kernel shares and roofline from one extra step with per-class CUDA events (kernels "
+                         "launched one by one, not from graphs: a short kernel's time includes the host's "
+                         "submission gap; roofline.back_to_back times the GEMM alone)",
         "roofline": roof,
         "kernel_time_share": share,
         "admm_iters_per_step": admm // a.steps,
