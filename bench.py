@@ -16,11 +16,12 @@ library's stream); `e2e` is the same through the C ABI call with host buffers,
 timed on the host; `plain_fp64` is the plain form on the same workload in the
 same run, and `time_to_optimum` a full branch-and-bound of a seeded G(100, 0.5)
 unit-weight instance (triangle cuts) in both forms.  `n512` compares the forms on
-G(512, 0.1) with integer weights in [-10, 10] (node throughput, bound agreement,
-and a time-capped branch-and-bound of the whole graph); `torus` bounds nodes of
-the 20 x 20 toroidal spin glass (n = 400, all three families) against the
-oracle's stored answers; `uneven_batch` bounds the roots of 2000 seeded
-independent subproblems of uneven order in one call.  Both
+G(512, 0.1) with integer weights in [-10, 10] (node throughput and bound
+agreement).  With --extended: `n512` adds a time-capped branch-and-bound of the
+whole graph in both forms, `torus` bounds nodes of the 20 x 20 toroidal spin
+glass (n = 400, all three families) against the oracle's stored answers, and
+`uneven_batch` bounds the roots of 2000 seeded independent subproblems of uneven
+order in one call.  Both
 arms print the same `config` (the workload); the reference arm (`--impl
 reference`) runs the reference's method on the host cores, one process per core
 started before the timed steps.
@@ -55,6 +56,9 @@ def _args():
     ap.add_argument("--cpu-sample", type=int, default=0, help="nodes in the CPU sample (0: one per core)")
     ap.add_argument("--cpu-only", action="store_true", help=argparse.SUPPRESS)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--extended", action="store_true",
+                    help="also the time-capped n = 512 trees, the torus block and the 2000-subproblem uneven batch "
+                         "(about ten more minutes)")
     return ap.parse_args()
 
 
@@ -202,7 +206,7 @@ DTYPES = {"learned": "bf16 digit planes (5 x 7-bit digits, products to ~5e-10) +
 N512 = "gnp512_int10"
 
 
-def n512_block(torch, M, stream, form, nodes=16, cap_s=60.0):
+def n512_block(torch, M, stream, form, nodes=16, cap_s=60.0, capped=True):
     """The n = 512 configuration (G(512, 0.1), integer weights in [-10, 10], all
     three cut families): node throughput of the chosen form and of the plain FP64
     form on the same nodes, the largest relative difference between their bounds,
@@ -235,6 +239,8 @@ def n512_block(torch, M, stream, form, nodes=16, cap_s=60.0):
     rel = [abs(x - y) / abs(y) for x, y in zip(bounds[form], bounds["fp64"])]
     out["speedup_vs_plain_fp64"] = out[form]["value"] / out["fp64"]["value"]
     out["bound_rel_diff_vs_fp64"] = {"max": max(rel), "mean": statistics.mean(rel)}
+    if not capped:
+        return out
     tto = {"cap_seconds": cap_s, "batch": 64}
     for f in (form, "fp64"):
         tc = _context(M, prm, wl["SL"], wl["n"], 64, f, profile=False)
@@ -507,9 +513,10 @@ def run_ours(a):
         tto["speedup"] = tto["fp64"]["seconds"] / tto[a.form]["seconds"]
         tto["same_optimum"] = tto["fp64"]["optimum"] == tto[a.form]["optimum"]
         if a.workload != N512:
-            n512 = n512_block(torch, M, stream, a.form)
-        torus = torus_block(torch, M, stream, a.form)
-        uneven = uneven_block(torch, M, stream, a.form)
+            n512 = n512_block(torch, M, stream, a.form, capped=a.extended)
+        if a.extended:
+            torus = torus_block(torch, M, stream, a.form)
+            uneven = uneven_block(torch, M, stream, a.form)
     cpu = None
     if not a.no_cpu_baseline:
         cores = host_cores()
