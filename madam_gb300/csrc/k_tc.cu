@@ -33,11 +33,13 @@
 // released), one thread of warp 0 issues the MMAs (waiting only for a stage to
 // land), so the MMAs of the next chunk queue behind those of this one.  All eight
 // warps drain the accumulators with tcgen05.ld (warp w: lanes 32 (w mod 4) .. +31,
-// columns 64 (w / 4) .. +63), each element once: its float-pair value, digit
-// planes and FP32 / FP64 forms are made in registers and stored to the element's
-// place (16 consecutive columns of a row per thread, vector stores of whole
-// 32-byte sectors) and to its mirror (one element per lane, consecutive across
-// the warp).  Every wait on an mbarrier is bounded: on expiry the CTA records an
+// columns 64 (w / 4) .. +63) in two phases.  Phase A sums each element's four
+// accumulators to a float pair; an off-diagonal tile stores its rows from
+// registers (16 consecutive columns per thread: vector stores of whole 32-byte
+// sectors), and a symmetric product stages the pairs, transposed, in shared
+// memory.  Phase B writes, again as whole rows, the diagonal tiles (every element
+// from the lower triangle, so the result is exactly symmetric) and the mirrors of
+// the off-diagonal tiles.  Every wait on an mbarrier is bounded: on expiry the CTA records an
 // error code, gives the TMA loads it still has in flight their own bounded wait,
 // skips the rest and releases its tensor memory.
 #include <cuda.h>
