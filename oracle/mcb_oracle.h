@@ -136,6 +136,8 @@ void orc_set_abstol(double abstol);
 void orc_set_ns_schedule(int k, const double *a, const double *b);
 /* relative residual at which the ADMM's linear solve stops (default 1e-15; <= 0 restores it) */
 void orc_set_cg_tol(double tol);
+/* on != 0: the ADMM's (B B^T + I) solve by a dense Cholesky factor instead of conjugate gradients */
+void orc_set_direct_solve(int on);
 /* largest eigenvalue as admm.c:731-752 computes it */
 double orc_lambda_max(int n, const double *A);
 /* basic SDP bound by the predictor-corrector IPM (ipm_mc_pk.c); returns iterations or -1 */

@@ -82,6 +82,7 @@ def lib():
     L.orc_set_abstol.argtypes = [C.c_double]
     L.orc_set_ns_schedule.argtypes = [C.c_int, C.c_void_p, C.c_void_p]
     L.orc_set_cg_tol.argtypes = [C.c_double]
+    L.orc_set_direct_solve.argtypes = [C.c_int]
     L.orc_lambda_max.restype = C.c_double
     L.orc_lambda_max.argtypes = [C.c_int, _dp]
     L.orc_ipm.argtypes = [_dp, C.c_int, _dp, _dp, _dp, C.POINTER(C.c_double)]
@@ -292,6 +293,12 @@ def set_ns_schedule(steps=None):
 def set_cg_tol(tol=None):
     """Relative residual of the ADMM's linear solve (None: the default 1e-15)."""
     lib().orc_set_cg_tol(tol if tol else 0.0)
+
+
+def set_direct_solve(on=True):
+    """The ADMM's (B B^T + I) solve by a dense Cholesky factor (the reference's CHOLMOD
+    arithmetic up to ordering and rounding) instead of the conjugate-gradient stand-in."""
+    lib().orc_set_direct_solve(1 if on else 0)
 
 
 def lambda_max(A, abstol=1e-8):

@@ -5,6 +5,7 @@
  * floating-point operations in the same order.
  * TEST INFRASTRUCTURE ONLY (see mcb_oracle.h).
  */
+#include <math.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -43,6 +44,7 @@ void orc_gram_build(int m, size_t nz, const int *rows, const int *cols, const do
     }
     qsort(tr, nt, sizeof(gtrip), gtrip_cmp);
     G->m = m;
+    G->L = NULL;
     G->rp = calloc((size_t)m + 1, sizeof(int));
     G->ci = malloc((nt + 1) * sizeof(int));
     G->v = malloc((nt + 1) * sizeof(double));
@@ -60,16 +62,59 @@ void orc_gram_build(int m, size_t nz, const int *rows, const int *cols, const do
 }
 
 void orc_gram_free(orc_gram *G) {
-    free(G->rp); free(G->ci); free(G->v);
-    G->rp = NULL; G->ci = NULL; G->v = NULL;
+    free(G->rp); free(G->ci); free(G->v); free(G->L);
+    G->rp = NULL; G->ci = NULL; G->v = NULL; G->L = NULL;
+}
+
+static int gram_direct = 0;
+void orc_set_direct_solve(int on) { gram_direct = on != 0; }
+
+/* dense lower Cholesky factor of G (column-major, m x m), left-looking; 0 on success */
+static int gram_factor(orc_gram *G) {
+    const int m = G->m;
+    double *L = calloc((size_t)m * m + 1, sizeof(double));
+    for (int i = 0; i < m; ++i)
+        for (int k = G->rp[i]; k < G->rp[i + 1]; ++k) L[i + (size_t)G->ci[k] * m] = G->v[k];
+    for (int j = 0; j < m; ++j) {
+        double *cj = L + (size_t)j * m;
+        for (int k = 0; k < j; ++k) {
+            const double *ck = L + (size_t)k * m;
+            const double ljk = ck[j];
+            if (ljk == 0.0) continue;
+            for (int i = j; i < m; ++i) cj[i] -= ck[i] * ljk;
+        }
+        if (!(cj[j] > 0.0)) { free(L); return -1; }
+        const double d = sqrt(cj[j]);
+        cj[j] = d;
+        for (int i = j + 1; i < m; ++i) cj[i] /= d;
+        for (int i = 0; i < j; ++i) cj[i] = 0.0;
+    }
+    G->L = L;
+    return 0;
 }
 
 /* squared relative residual at which the solve stops (1e-15 by default) */
 static double gram_tol2 = 1e-30;
 void orc_set_cg_tol(double tol) { gram_tol2 = tol > 0 ? tol * tol : 1e-30; }
 
-void orc_gram_solve(const orc_gram *G, const double *b, double *x) {
+void orc_gram_solve(orc_gram *G, const double *b, double *x) {
     int m = G->m;
+    if (gram_direct && (G->L || gram_factor(G) == 0)) {
+        const double *L = G->L;
+        for (int i = 0; i < m; ++i) x[i] = b[i];
+        for (int j = 0; j < m; ++j) {  /* L y = b */
+            const double *cj = L + (size_t)j * m;
+            x[j] /= cj[j];
+            for (int i = j + 1; i < m; ++i) x[i] -= cj[i] * x[j];
+        }
+        for (int j = m - 1; j >= 0; --j) {  /* L^T x = y */
+            const double *cj = L + (size_t)j * m;
+            double acc = x[j];
+            for (int i = j + 1; i < m; ++i) acc -= cj[i] * x[i];
+            x[j] = acc / cj[j];
+        }
+        return;
+    }
     double *r = malloc(((size_t)m + 1) * sizeof(double)), *p = malloc(((size_t)m + 1) * sizeof(double));
     double *q = malloc(((size_t)m + 1) * sizeof(double));
     double bb = 0.0;

@@ -240,6 +240,34 @@ def test_linear_solve_tolerance_slack(orc, gpu_lib):
     assert abs(out[1e-8][0] - out[1e-10][0]) <= 1e-8 * abs(out[1e-10][0]), out
 
 
+@pytest.mark.parametrize("n,p,wts,seed,fixed,pent,hept", [
+    (40, 0.5, "one", 2, {3: 1, 11: 0}, 1, 0),
+    (64, 0.5, "pm1", 4, {}, 0, 0),
+    (80, 0.1, "int10", 5, {7: 1}, 1, 1),
+])
+def test_cg_stand_in_matches_a_direct_factorisation(orc, n, p, wts, seed, fixed, pent, hept):
+    """The oracle (and the reference build here) solve (B B^T + I) t = r by conjugate
+    gradients to 1e-15 where the reference factors it with CHOLMOD (admm.c:480-487,546).
+    With a dense Cholesky factor in its place the node bound runs the same rounds,
+    ADMM iterations and cuts and ends within 1e-13: the stand-in does not move the
+    reference's answer."""
+    nv, e, w = G.gnp(n, p, wts, seed=seed)
+    SL = G.extended_laplacian(nv, e, w).ravel(order="F")
+    prm = orc.shipped_params(include_Pent=pent, include_Hepta=hept, use_diff=0)
+    out = []
+    try:
+        for direct in (False, True):
+            orc.set_direct_solve(direct)
+            oc = orc.Ctx(prm, SL, nv, rng=orc.RNG_COUNTER, topk=orc.TOPK_CANONICAL, canon_sign=1)
+            b, st = oc.evaluate(orc.make_node(nv - 1, fixed), rank=1)
+            out.append((b, (st.outer_iters, st.admm_iters, st.n_tri, st.n_pent, st.n_hept)))
+            oc.close()
+    finally:
+        orc.set_direct_solve(False)
+    assert out[0][1] == out[1][1] and out[0][1][1] > 0, out
+    assert abs(out[0][0] - out[1][0]) <= 1e-13 * abs(out[1][0]), out
+
+
 # ---- numpy restatements of the operators ------------------------------------
 def _np_op_B(X, tri, pent, hept):
     y = []
