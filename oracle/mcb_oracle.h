@@ -138,6 +138,8 @@ void orc_set_ns_schedule(int k, const double *a, const double *b);
 void orc_set_cg_tol(double tol);
 /* on != 0: the ADMM's (B B^T + I) solve by a dense Cholesky factor instead of conjugate gradients */
 void orc_set_direct_solve(int on);
+/* append every matrix W the ADMM projects to the file at path (int n, n x n doubles); NULL closes */
+void orc_set_projection_dump(const char *path);
 /* largest eigenvalue as admm.c:731-752 computes it */
 double orc_lambda_max(int n, const double *A);
 /* basic SDP bound by the predictor-corrector IPM (ipm_mc_pk.c); returns iterations or -1 */

@@ -83,6 +83,7 @@ def lib():
     L.orc_set_ns_schedule.argtypes = [C.c_int, C.c_void_p, C.c_void_p]
     L.orc_set_cg_tol.argtypes = [C.c_double]
     L.orc_set_direct_solve.argtypes = [C.c_int]
+    L.orc_set_projection_dump.argtypes = [C.c_char_p]
     L.orc_lambda_max.restype = C.c_double
     L.orc_lambda_max.argtypes = [C.c_int, _dp]
     L.orc_ipm.argtypes = [_dp, C.c_int, _dp, _dp, _dp, C.POINTER(C.c_double)]
@@ -293,6 +294,11 @@ def set_ns_schedule(steps=None):
 def set_cg_tol(tol=None):
     """Relative residual of the ADMM's linear solve (None: the default 1e-15)."""
     lib().orc_set_cg_tol(tol if tol else 0.0)
+
+
+def set_projection_dump(path=None):
+    """Append every matrix W the ADMM projects to a file (int n, then n x n doubles); None closes it."""
+    lib().orc_set_projection_dump(path.encode() if path else None)
 
 
 def set_direct_solve(on=True):

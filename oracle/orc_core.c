@@ -619,6 +619,14 @@ static double fro_lower(const double *A, int n) {
     return orc_la.dlansy("F", "L", &n, A, &n, dummy, 1, 1);
 }
 
+/* Studies of the projection's input: every W the ADMM projects is appended to this
+ * file (int n, then the n x n column-major doubles) while it is open. */
+static FILE *proj_dump = NULL;
+void orc_set_projection_dump(const char *path) {
+    if (proj_dump) fclose(proj_dump);
+    proj_dump = path ? fopen(path, "wb") : NULL;
+}
+
 /* ADMM_solver, admm.c:49-771.  Works on c->X, c->y, c->Q, c->t, c->s, c->u and
  * the cut lists; leaves the safe bound in c->f and the heuristic's factor in c->Z. */
 int orc_admm(orc_ctx *c, double *sigma, double tol, int *nbit) {
@@ -661,6 +669,10 @@ int orc_admm(orc_ctx *c, double *sigma, double tol, int *nbit) {
         orc_op_Bt(n, X, c->ntri, c->tri, c->npent, c->pent, c->nhept, c->hept, t);
         /* project_SDP(PP): X <- X_+ (lower), Q <- X_+ - W */
         memcpy(tmp, X, nn * sizeof(double));
+        if (proj_dump) {
+            fwrite(&n, sizeof(int), 1, proj_dump);
+            fwrite(tmp, sizeof(double), (size_t)n * n, proj_dump);
+        }
         int M = orc_project(n, tmp, X, Q, c->Z, evals, c->canon_sign);
         if (M < 0) { err_flag = 1; break; }
         c->M = M;
