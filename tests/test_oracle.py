@@ -268,6 +268,32 @@ def test_cg_stand_in_matches_a_direct_factorisation(orc, n, p, wts, seed, fixed,
     assert abs(out[0][0] - out[1][0]) <= 1e-13 * abs(out[1][0]), out
 
 
+def test_projection_dump_records_every_admm_projection(orc, tmp_path):
+    """The study hook orc_set_projection_dump appends each matrix the ADMM projects:
+    one record per ADMM iteration, of the subproblem's order."""
+    nv, e, w = G.gnp(40, 0.5, "one", seed=2)
+    SL = G.extended_laplacian(nv, e, w).ravel(order="F")
+    path = str(tmp_path / "w.bin")
+    try:
+        orc.set_projection_dump(path)
+        oc = orc.Ctx(orc.shipped_params(include_Pent=0, include_Hepta=0, use_diff=0), SL, nv)
+        _, st = oc.evaluate(orc.make_node(nv - 1), rank=1)
+        oc.close()
+    finally:
+        orc.set_projection_dump(None)
+    raw = open(path, "rb").read()
+    count, off, n0 = 0, 0, None
+    while off < len(raw):
+        n = int(np.frombuffer(raw, dtype=np.int32, count=1, offset=off)[0])
+        n0 = n if n0 is None else n0
+        assert n == n0
+        W = np.frombuffer(raw, dtype=np.float64, count=n * n, offset=off + 4)
+        assert np.isfinite(W).all()
+        off += 4 + 8 * n * n
+        count += 1
+    assert off == len(raw) and n0 == nv and count == st.admm_iters > 0
+
+
 # ---- numpy restatements of the operators ------------------------------------
 def _np_op_B(X, tri, pent, hept):
     y = []
